@@ -1,0 +1,73 @@
+"""ctypes binding of libhlbl_gb300.so (the C ABI of include/hlbl_gb300.h).
+
+The library is the product: there is no fallback. If it is missing this
+module raises at import, naming the build command.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from .build import LIB
+
+I4 = C.c_int * 4
+
+
+class HlblError(RuntimeError):
+    """A C-ABI call returned a nonzero status."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"hlbl error {code}: {msg}")
+        self.code = code
+
+
+def _load() -> C.CDLL:
+    if not os.path.exists(LIB):
+        raise ImportError(f"{LIB} is missing: build it with `python -m hlbl_gb300.build`")
+    lib = C.CDLL(LIB)
+    vp, i4p, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)
+    sigs = {
+        "hlbl_last_error": (C.c_char_p, []),
+        "hlbl_version": (C.c_char_p, []),
+        "hlbl_ctx_create": (C.c_int, [C.POINTER(vp), i4p, i4p, i4p, C.c_double, C.c_int]),
+        "hlbl_ctx_destroy": (None, [vp]),
+        "hlbl_ctx_set_stream": (C.c_int, [vp, vp]),
+        "hlbl_kernel_sum": (C.c_int, [vp, vp, vp, i4p, i4p, C.c_double, C.c_int, dp]),
+        "hlbl_kernel_sum_async": (C.c_int, [vp, vp, vp, i4p, i4p, C.c_double, C.c_int, vp]),
+        "hlbl_cu_dzu_dzsu": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, i4p, i4p, i4p, i4p]),
+        "hlbl_cu_4pt_contraction": (C.c_int, [vp, vp, vp, vp, vp, vp, C.c_int, i4p, i4p,
+                                              C.c_double, i4p, i4p, i4p]),
+        "hlbl_insert_gammas": (C.c_int, [vp, vp, vp, vp, vp]),
+        "hlbl_reserve_kernel_memory": (C.c_int, [vp, C.POINTER(C.c_size_t)]),
+        "hlbl_fill_random_block": (C.c_int, [vp, vp, C.c_uint64]),
+        "hlbl_fill_gaussian_block": (C.c_int, [vp, vp, C.c_uint64]),
+        "hlbl_source_seed": (C.c_uint64, [C.c_uint64, i4p]),
+        "hlbl_block_length": (C.c_size_t, [vp]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        raise HlblError(rc, lib.hlbl_last_error().decode())
+
+
+def i4(v) -> "C.Array":
+    v = [int(a) for a in v]
+    if len(v) != 4:
+        raise ValueError("expected 4 coordinates (t, x, y, z)")
+    return I4(*v)
+
+
+def ptr(x) -> int:
+    """Device address of a torch tensor (or an int address)."""
+    if isinstance(x, int):
+        return x
+    return int(x.data_ptr())

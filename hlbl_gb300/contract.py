@@ -1,0 +1,142 @@
+"""The Contractor: hlbl::Contractor's interface (include/hlbl/contract.hpp:42-94
+of the reference) over the C ABI of libhlbl_gb300.so.
+
+Propagator blocks are device buffers (torch tensors or raw device addresses)
+in the reference's layout [2][12][V][24] doubles. One Contractor per lattice;
+it owns its work buffers and a CUDA stream.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from ._lib import check, i4, lib, ptr
+
+FP64 = 0  # per-site products in FP64 (the exact path)
+FP32 = 1  # per-site products in FP32, FP64 site and volume sums
+HBARC_MEV_FM = 197.3269804  # include/hlbl/physics.hpp:9
+
+
+def xunit(muon_mass_mev: float, lattice_spacing_fm: float) -> float:
+    """m_mu a, the lattice unit in units of the muon mass (physics.hpp:12-14)."""
+    return muon_mass_mev / HBARC_MEV_FM * lattice_spacing_fm
+
+
+def _prec(p) -> int:
+    if p in (FP64, "fp64"):
+        return FP64
+    if p in (FP32, "fp32"):
+        return FP32
+    raise ValueError(f"precision must be fp64 or fp32, not {p!r}")
+
+
+class Contractor:
+    """Kernel sums of pairs of point sources (src/contract.cpp of the reference)."""
+
+    def __init__(self, global_extents, local_extents=None, proc_coords=(0, 0, 0, 0),
+                 lam: float = 0.4, device: int = 0):
+        local_extents = global_extents if local_extents is None else local_extents
+        h = C.c_void_p()
+        check(lib.hlbl_ctx_create(C.byref(h), i4(global_extents), i4(local_extents),
+                                  i4(proc_coords), C.c_double(lam), int(device)))
+        self._h = h
+        self.global_extents = tuple(int(a) for a in global_extents)
+        self.local_extents = tuple(int(a) for a in local_extents)
+        self.proc_coords = tuple(int(a) for a in proc_coords)
+        self.lam = lam
+        self.device = device
+
+    # -- lifetime --------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib.hlbl_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    @property
+    def volume(self) -> int:
+        v = 1
+        for a in self.local_extents:
+            v *= a
+        return v
+
+    @property
+    def block_length(self) -> int:
+        """Doubles in one propagator block (provider.hpp:18-20)."""
+        return int(lib.hlbl_block_length(self._h))
+
+    def set_stream(self, stream) -> None:
+        """Run on a CUDA stream (torch.cuda.Stream, a raw handle, or None)."""
+        raw = getattr(stream, "cuda_stream", stream)
+        check(lib.hlbl_ctx_set_stream(self._h, C.c_void_p(raw) if raw else None))
+
+    # -- the hot path ----------------------------------------------------
+    def kernel_sum(self, d_fwd_src, d_fwd_y, gsx, yv, xunit: float, precision=FP64):
+        """Both flavours' kernel sums of the pair (x = gsx, y = gsx + yv).
+
+        Contractor::kernel_sum, src/contract.cpp:104-114 (one rank; with more
+        ranks sum the returned values over ranks)."""
+        out = (C.c_double * 2)()
+        check(lib.hlbl_kernel_sum(self._h, ptr(d_fwd_src), ptr(d_fwd_y), i4(gsx), i4(yv),
+                                  C.c_double(xunit), _prec(precision), out))
+        return out[0], out[1]
+
+    def kernel_sum_async(self, d_fwd_src, d_fwd_y, gsx, yv, xunit: float, d_out,
+                         precision=FP64) -> None:
+        """As kernel_sum, results written to the device buffer d_out[2]."""
+        check(lib.hlbl_kernel_sum_async(self._h, ptr(d_fwd_src), ptr(d_fwd_y), i4(gsx), i4(yv),
+                                        C.c_double(xunit), _prec(precision), ptr(d_out)))
+
+    # -- the vendored launchers (kernels/cuda_lattice.h:49-57) -------------
+    def cu_dzu_dzsu(self, d_dzu, d_dzsu, fwd_src, fwd_y, iflavor, proc_coords, gsx,
+                    global_geom, local_geom) -> None:
+        check(lib.hlbl_cu_dzu_dzsu(self._h, ptr(d_dzu), ptr(d_dzsu), ptr(fwd_src), ptr(fwd_y),
+                                   int(iflavor), i4(proc_coords), i4(gsx), i4(global_geom),
+                                   i4(local_geom)))
+
+    def cu_4pt_contraction(self, d_kernel_sum, d_g_dzu, d_g_dzsu, fwd_src, fwd_y, iflavor,
+                           proc_coords, gsx, xunit, yv, global_geom, local_geom) -> None:
+        check(lib.hlbl_cu_4pt_contraction(self._h, ptr(d_kernel_sum), ptr(d_g_dzu),
+                                          ptr(d_g_dzsu), ptr(fwd_src), ptr(fwd_y), int(iflavor),
+                                          i4(proc_coords), i4(gsx), C.c_double(xunit), i4(yv),
+                                          i4(global_geom), i4(local_geom)))
+
+    def insert_gammas(self, d_dzu, d_dzsu, d_g_dzu, d_g_dzsu) -> None:
+        """contract.cpp:58-77 on the device."""
+        check(lib.hlbl_insert_gammas(self._h, ptr(d_dzu), ptr(d_dzsu), ptr(d_g_dzu),
+                                     ptr(d_g_dzsu)))
+
+    def reserve_kernel_memory(self) -> int:
+        """Contractor::reserve_kernel_memory (contract.cpp:158-197)."""
+        n = C.c_size_t()
+        check(lib.hlbl_reserve_kernel_memory(self._h, C.byref(n)))
+        return int(n.value)
+
+    def pieces_2p2(self, *args, **kwargs):
+        """Contractor::pieces_2p2 (contract.cpp:116-156) is not part of this
+        library: the 2+2 pieces are a different contraction."""
+        raise NotImplementedError("the 2+2 pieces (compute_2p2_gpu) are not implemented here")
+
+    # -- fixtures (src/provider.cpp) ---------------------------------------
+    def fill_random_block(self, d_out, seed: int) -> None:
+        """fill_random_block with a per-source seed, on the device."""
+        check(lib.hlbl_fill_random_block(self._h, ptr(d_out), C.c_uint64(seed)))
+
+    def fill_gaussian_block(self, d_out, seed: int) -> None:
+        check(lib.hlbl_fill_gaussian_block(self._h, ptr(d_out), C.c_uint64(seed)))
+
+    @staticmethod
+    def source_seed(run_seed: int, gsx) -> int:
+        """RandomProvider's per-source seed (provider.cpp:59-64)."""
+        return int(lib.hlbl_source_seed(C.c_uint64(run_seed), i4(gsx)))

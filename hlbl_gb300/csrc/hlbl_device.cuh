@@ -1,0 +1,97 @@
+// hlbl_device.cuh -- device-side building blocks shared by the kernels:
+// gamma matrices of the cvc basis as monomial spin matrices, the lattice
+// coordinate rules, and the kernel-parameter structs.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "hlbl_gb300_qed.h"
+
+namespace hg {
+
+// ---- gamma matrices -----------------------------------------------------
+// The cvc basis of the reference (src/gamma.cpp:7-45, cuda_lattice.cu:16-51)
+// acts on a spinor v[spin][colour] as (gamma_g v)[s] = i^ph(g,s) v[src(g,s)]:
+// every row has a single entry, a power of i. g = 0..3 and 5 (4 is unused).
+// The two tables below restate the reference's permutation/sign tables in
+// that form; tests check them against the reference's apply_gamma.
+__host__ __device__ constexpr int gam_src(int g, int s) {
+  // gamma_0, gamma_3: spins 0<->2, 1<->3; gamma_1, gamma_2: 0<->3, 1<->2
+  return (g == 0 || g == 3) ? (s ^ 2) : ((g == 1 || g == 2) ? (3 - s) : s);
+}
+__host__ __device__ constexpr int gam_ph(int g, int s) {
+  // powers of i: g0 {2,2,2,2} g1 {3,3,1,1} g2 {2,0,0,2} g3 {3,1,1,3} g5 {0,0,2,2}
+  return g == 0 ? 2
+       : g == 1 ? (s < 2 ? 3 : 1)
+       : g == 2 ? ((s == 0 || s == 3) ? 2 : 0)
+       : g == 3 ? ((s == 0 || s == 3) ? 3 : 1)
+       : g == 5 ? (s < 2 ? 0 : 2)
+       : 0;
+}
+// gamma_5 gamma_mu: (g5 g_mu v)[s] = i^(ph_mu(s) + ph_5(s)) v[src_mu(s)]
+__host__ __device__ constexpr int g5g_src(int mu, int s) { return gam_src(mu, s); }
+__host__ __device__ constexpr int g5g_ph(int mu, int s) { return (gam_ph(mu, s) + gam_ph(5, s)) & 3; }
+// gamma_mu gamma_5: (g_mu g5 v)[s] = i^(ph_mu(s) + ph_5(src_mu(s))) v[src_mu(s)]
+__host__ __device__ constexpr int gg5_src(int mu, int s) { return gam_src(mu, s); }
+__host__ __device__ constexpr int gg5_ph(int mu, int s) {
+  return (gam_ph(mu, s) + gam_ph(5, gam_src(mu, s))) & 3;
+}
+
+// z * i^ph
+template <typename T>
+__host__ __device__ __forceinline__ void mul_iph(int ph, T re, T im, T& ore, T& oim) {
+  switch (ph & 3) {
+    case 0: ore = re;  oim = im;  break;
+    case 1: ore = -im; oim = re;  break;
+    case 2: ore = -re; oim = -im; break;
+    default: ore = im; oim = -re; break;
+  }
+}
+
+// ---- coordinate rules (cuda_lattice.cu:128-154) -------------------------
+// [-L/2, L/2) with L/2 -> -L/2: every QED kernel argument
+__host__ __device__ __forceinline__ int coord_map(int xi, int L) { return xi >= L / 2 ? xi - L : xi; }
+// L/2 -> 0: the odd coordinate weights z_rho, x_rho only
+__host__ __device__ __forceinline__ int coord_map_zerohalf(int xi, int L) {
+  return xi > L / 2 ? xi - L : (xi < L / 2 ? xi : 0);
+}
+__host__ __device__ __forceinline__ int mod_pos(int a, int L) {
+  int const r = a % L;
+  return r < 0 ? r + L : r;
+}
+// minimum-image difference a - b
+__host__ __device__ __forceinline__ int coord_map_diff(int a, int b, int L) {
+  return coord_map(mod_pos(a - b, L), L);
+}
+
+// ---- geometry passed to every kernel ------------------------------------
+struct Geometry {
+  int local[4];   // T, LX, LY, LZ of this rank's sub-lattice
+  int global[4];  // of the whole lattice
+  int pc[4];      // this rank's process-grid coordinates
+  long long V;    // local volume
+};
+
+// Position relative to the source x = gsx of local site `site`, folded
+// into [0, L) per direction (cuda_lattice.cu:196-201, 315-318).
+__device__ __forceinline__ void rel_coords(const Geometry& g, const int gsx[4], long long site,
+                                           int rel[4]) {
+  long long s = site;
+  int c[4];
+  c[3] = (int)(s % g.local[3]); s /= g.local[3];
+  c[2] = (int)(s % g.local[2]); s /= g.local[2];
+  c[1] = (int)(s % g.local[1]); s /= g.local[1];
+  c[0] = (int)s;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    int const v = c[r] + g.pc[r] * g.local[r] - gsx[r];
+    rel[r] = (v + g.global[r]) % g.global[r];
+  }
+}
+
+// (rho, sigma) of the six pairs k, cuda_lattice.cu:52-60
+__host__ __device__ constexpr int comb_rho(int k) { return k < 3 ? 0 : (k < 5 ? 1 : 2); }
+__host__ __device__ constexpr int comb_sigma(int k) { return k < 3 ? k + 1 : (k < 5 ? k - 1 : 3); }
+
+}  // namespace hg

@@ -1,0 +1,421 @@
+/*
+ * hlbl_oracle.c -- TEST INFRASTRUCTURE. The CPU oracle for the connected HLbL
+ * kernel sum. Only the tests, the smoke check and bench.py's CPU-baseline leg
+ * load it, as the checker; the product never calls it.
+ *
+ * A plain FP64 restatement (OpenMP over sites) of the reference's algorithm:
+ *
+ *   oracle_dzu_dzsu      pass 1, kernels/cuda_lattice.cu:160-262 (ker_dzu_dzsu)
+ *   oracle_insert_gammas host gamma insertion, src/contract.cpp:18-24, 58-77
+ *   oracle_4pt           pass 2, kernels/cuda_lattice.cu:277-484
+ *                        (ker_4pt_contraction) with the QED calls of :266-275
+ *   oracle_kernel_sum    Contractor::kernel_sum, src/contract.cpp:104-114
+ *   oracle_fill_*        the block fixtures, src/provider.cpp:25-69
+ *
+ * The loops follow the reference's order of operations per site; loop
+ * invariants are hoisted (gamma-rotated spinors are formed once per site
+ * instead of once per inner iteration), which changes no value. Sums over
+ * sites use per-thread partials reduced in thread order, so a run is
+ * deterministic for a given thread count. The QED kernel is the project's
+ * stand-in (include/hlbl_gb300_qed.h), as KQED is not available.
+ *
+ * Parity pin: these functions are checked against the reference's own
+ * sources compiled as a host emulation (oracle/ref_host) through the golden
+ * fixtures in tests/golden.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "hlbl_gb300_qed.h"
+#include "hlbl_gb300_rng.h"
+
+/* ---- gamma matrices in the cvc basis (src/gamma.cpp:7-45,
+ * kernels/cuda_lattice.cu:16-51), as monomial spin matrices:
+ * (gamma_g v)[s][c] = i^ph[g][s] * v[src[g][s]][c]. Row 4 is unused. */
+static const int g_src[6][4] = {{2, 3, 0, 1}, {3, 2, 1, 0}, {3, 2, 1, 0},
+                                {2, 3, 0, 1}, {0, 1, 2, 3}, {0, 1, 2, 3}};
+static const int g_ph[6][4] = {{2, 2, 2, 2}, {3, 3, 1, 1}, {2, 0, 0, 2},
+                               {3, 1, 1, 3}, {0, 0, 0, 0}, {0, 0, 2, 2}};
+
+/* out = gamma_g in (24 doubles, 12 complex, index 3*spin + colour) */
+static void apply_gamma(int g, const double* in, double* out) {
+  for (int s = 0; s < 4; ++s) {
+    int const j = g_src[g][s], ph = g_ph[g][s];
+    for (int c = 0; c < 3; ++c) {
+      double const re = in[2 * (3 * j + c)], im = in[2 * (3 * j + c) + 1];
+      double* o = out + 2 * (3 * s + c);
+      switch (ph) {
+        case 0: o[0] = re;  o[1] = im;  break;
+        case 1: o[0] = -im; o[1] = re;  break;
+        case 2: o[0] = -re; o[1] = -im; break;
+        default: o[0] = im; o[1] = -re; break;
+      }
+    }
+  }
+}
+/* in place: gamma_5 (spins 2 and 3 change sign), cuda_lattice.cu:96-100 */
+static void times_g5(double* v) {
+  for (int i = 12; i < 24; ++i) v[i] = -v[i];
+}
+
+void oracle_apply_gamma(int g, const double* in, double* out) { apply_gamma(g, in, out); }
+
+/* ---- coordinate rules, cuda_lattice.cu:128-154 (VENDORED.md: one rule,
+ * [-L/2, L/2), for every QED kernel argument; L/2 -> 0 only for the odd
+ * coordinate weights) */
+int oracle_coord_map(int xi, int L) { return xi >= L / 2 ? xi - L : xi; }
+int oracle_coord_map_zerohalf(int xi, int L) {
+  return xi > L / 2 ? xi - L : (xi < L / 2 ? xi : 0);
+}
+int oracle_mod_pos(int a, int L) {
+  int const r = a % L;
+  return r < 0 ? r + L : r;
+}
+int oracle_coord_map_diff(int a, int b, int L) {
+  return oracle_coord_map(oracle_mod_pos(a - b, L), L);
+}
+
+static int n_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+static int thread_id(void) {
+#ifdef _OPENMP
+  return omp_get_thread_num();
+#else
+  return 0;
+#endif
+}
+
+void oracle_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+int oracle_get_threads(void) { return n_threads(); }
+
+/* ---- fixtures (src/provider.cpp) ---- */
+
+/* fill_random_block (provider.cpp:25-57): layout ((f*12+ia)*V + site)*24 + c,
+ * site = ((t*LX+x)*LY+y)*LZ+z local, values keyed by the global site. */
+void oracle_fill_random_block(const int local[4], const int pc[4], uint64_t seed,
+                              double* out) {
+  size_t const V = (size_t)local[0] * local[1] * local[2] * local[3];
+#pragma omp parallel for schedule(static)
+  for (long long site = 0; site < (long long)V; ++site) {
+    int const z = (int)(site % local[3]);
+    int const y = (int)((site / local[3]) % local[2]);
+    int const x = (int)((site / ((size_t)local[3] * local[2])) % local[1]);
+    int const t = (int)(site / ((size_t)local[3] * local[2] * local[1]));
+    uint64_t const g = hlbl_rng_site_key(pc[0] * local[0] + t, pc[1] * local[1] + x,
+                                         pc[2] * local[2] + y, pc[3] * local[3] + z);
+    for (int f = 0; f < 2; ++f)
+      for (int ia = 0; ia < 12; ++ia)
+        for (int c = 0; c < 24; ++c)
+          out[((size_t)(f * 12 + ia) * V + (size_t)site) * 24 + c] =
+              hlbl_rng_uniform_entry(seed, g, f, ia, c);
+  }
+}
+
+/* RandomProvider::compute's per-source seed (provider.cpp:59-64). */
+uint64_t oracle_source_seed(uint64_t seed, const int gsx[4]) {
+  return hlbl_rng_source_seed(seed, gsx);
+}
+
+/* The Gaussian fixture of the benchmark configurations, same layout. */
+void oracle_fill_gaussian_block(const int local[4], const int pc[4], uint64_t seed,
+                                double* out) {
+  size_t const V = (size_t)local[0] * local[1] * local[2] * local[3];
+#pragma omp parallel for schedule(static)
+  for (long long site = 0; site < (long long)V; ++site) {
+    int const z = (int)(site % local[3]);
+    int const y = (int)((site / local[3]) % local[2]);
+    int const x = (int)((site / ((size_t)local[3] * local[2])) % local[1]);
+    int const t = (int)(site / ((size_t)local[3] * local[2] * local[1]));
+    uint64_t const g = hlbl_rng_site_key(pc[0] * local[0] + t, pc[1] * local[1] + x,
+                                         pc[2] * local[2] + y, pc[3] * local[3] + z);
+    for (int f = 0; f < 2; ++f)
+      for (int ia = 0; ia < 12; ++ia)
+        for (int c = 0; c < 12; ++c) {
+          double* o = out + ((size_t)(f * 12 + ia) * V + (size_t)site) * 24 + 2 * c;
+          hlbl_rng_gaussian_entry(seed, g, f, ia, c, o, o + 1);
+        }
+  }
+}
+
+/* ---- the QED kernel (cuda_lattice.cu:266-275 calls QED_Mkernel_L2) ---- */
+void oracle_qed_kernel(double lambda, const double x[4], const double y[4], double* kerv) {
+  hlbl_qed_params p;
+  hlbl_qed_params_init(&p, lambda);
+  hlbl_qed_kernel(&p, x, y, (double(*)[4][4][4])kerv);
+}
+void oracle_qed_weights(double lambda, double X, double c, double Y, double* w) {
+  hlbl_qed_params p;
+  hlbl_qed_params_init(&p, lambda);
+  hlbl_qed_weights(&p, X, c, Y, w);
+}
+
+static void site_coords(size_t ix, const int local[4], int coord[4]) {
+  coord[3] = (int)(ix % local[3]);
+  coord[2] = (int)((ix / local[3]) % local[2]);
+  coord[1] = (int)((ix / ((size_t)local[3] * local[2])) % local[1]);
+  coord[0] = (int)(ix / ((size_t)local[3] * local[2] * local[1]));
+}
+
+static const int comb[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+
+/* ---- pass 1: ker_dzu_dzsu (cuda_lattice.cu:160-262) -------------------
+ * dzu[k][ia][ib]  += sum_z conj(fwd_y[1-f][ib](z)) . (z_rho g5 g_sigma - z_sigma g5 g_rho) fwd_src[f][ia](z)
+ * dzsu[s][ia][ib] += sum_z conj(fwd_y[1-f][ib](z)) . g5 g_s fwd_src[f][ia](z)
+ * z_rho = coord_map_zerohalf((z - gsx)_rho mod L_rho). Adds into dzu, dzsu. */
+void oracle_dzu_dzsu(double* dzu, double* dzsu, const double* fwd_src, const double* fwd_y,
+                     int iflavor, const int pc[4], const int gsx[4], const int global[4],
+                     const int local[4]) {
+  size_t const V = (size_t)local[0] * local[1] * local[2] * local[3];
+  int const nt = n_threads();
+  double* part = (double*)calloc((size_t)nt * 2880, sizeof(double));
+#pragma omp parallel
+  {
+    double* acc_u = part + (size_t)thread_id() * 2880; /* [6][12][12][2] */
+    double* acc_s = acc_u + 1728;                       /* [4][12][12][2] */
+#pragma omp for schedule(static)
+    for (long long iz = 0; iz < (long long)V; ++iz) {
+      int coord[4], zf[4];
+      site_coords((size_t)iz, local, coord);
+      for (int r = 0; r < 4; ++r) {
+        int zr = coord[r] + pc[r] * local[r] - gsx[r];
+        zr = (zr + global[r]) % global[r];
+        zf[r] = oracle_coord_map_zerohalf(zr, global[r]);
+      }
+      for (int ia = 0; ia < 12; ++ia) {
+        const double* u = fwd_src + ((size_t)(iflavor * 12 + ia) * V + (size_t)iz) * 24;
+        double t[4][24]; /* g5 g_s u */
+        for (int s = 0; s < 4; ++s) {
+          apply_gamma(s, u, t[s]);
+          times_g5(t[s]);
+        }
+        for (int k = 0; k < 6; ++k) {
+          int const rho = comb[k][0], sigma = comb[k][1];
+          double const fr = zf[rho], fs = zf[sigma];
+          for (int ib = 0; ib < 12; ++ib) {
+            const double* yb =
+                fwd_y + ((size_t)((1 - iflavor) * 12 + ib) * V + (size_t)iz) * 24;
+            double re = 0, im = 0;
+            for (int i = 0; i < 12; ++i) {
+              double const yr = yb[2 * i], yi = yb[2 * i + 1];
+              double const sr = t[sigma][2 * i] * fr - t[rho][2 * i] * fs;
+              double const si = t[sigma][2 * i + 1] * fr - t[rho][2 * i + 1] * fs;
+              re += yr * sr + yi * si;
+              im += yr * si - yi * sr;
+            }
+            acc_u[((k * 12 + ia) * 12 + ib) * 2] += re;
+            acc_u[((k * 12 + ia) * 12 + ib) * 2 + 1] += im;
+          }
+        }
+        for (int s = 0; s < 4; ++s) {
+          for (int ib = 0; ib < 12; ++ib) {
+            const double* yb =
+                fwd_y + ((size_t)((1 - iflavor) * 12 + ib) * V + (size_t)iz) * 24;
+            double re = 0, im = 0;
+            for (int i = 0; i < 12; ++i) {
+              double const yr = yb[2 * i], yi = yb[2 * i + 1];
+              re += yr * t[s][2 * i] + yi * t[s][2 * i + 1];
+              im += yr * t[s][2 * i + 1] - yi * t[s][2 * i];
+            }
+            acc_s[((s * 12 + ia) * 12 + ib) * 2] += re;
+            acc_s[((s * 12 + ia) * 12 + ib) * 2 + 1] += im;
+          }
+        }
+      }
+    }
+  }
+  for (int th = 0; th < nt; ++th) {
+    for (int i = 0; i < 1728; ++i) dzu[i] += part[(size_t)th * 2880 + i];
+    for (int i = 0; i < 1152; ++i) dzsu[i] += part[(size_t)th * 2880 + 1728 + i];
+  }
+  free(part);
+}
+
+/* ---- host glue (contract.cpp:58-77): g_dzu[k][mu][ia] = g_mu g5 dzu[k][ia],
+ * g_dzsu[s][mu][ia] = g_mu g5 dzsu[s][ia] (gamma on the 24-vector over ib) */
+void oracle_insert_gammas(const double* dzu, const double* dzsu, double* g_dzu,
+                          double* g_dzsu) {
+  double t[24];
+  for (int k = 0; k < 6; ++k)
+    for (int ia = 0; ia < 12; ++ia)
+      for (int mu = 0; mu < 4; ++mu) {
+        memcpy(t, dzu + (k * 12 + ia) * 24, sizeof t);
+        times_g5(t);
+        apply_gamma(mu, t, g_dzu + ((k * 4 + mu) * 12 + ia) * 24);
+      }
+  for (int s = 0; s < 4; ++s)
+    for (int ia = 0; ia < 12; ++ia)
+      for (int mu = 0; mu < 4; ++mu) {
+        memcpy(t, dzsu + (s * 12 + ia) * 24, sizeof t);
+        times_g5(t);
+        apply_gamma(mu, t, g_dzsu + ((s * 4 + mu) * 12 + ia) * 24);
+      }
+}
+
+/* ---- pass 2: ker_4pt_contraction (cuda_lattice.cu:277-484) ------------
+ * Returns the sum over this rank's sites; the caller adds it to its
+ * accumulator as the reference's atomicAdd does. */
+double oracle_4pt(const double* g_dzu, const double* g_dzsu, const double* fwd_src,
+                  const double* fwd_y, int iflavor, const int pc[4], const int gsx[4],
+                  double xunit, const int yv[4], double lambda, const int global[4],
+                  const int local[4]) {
+  size_t const V = (size_t)local[0] * local[1] * local[2] * local[3];
+  int const nt = n_threads();
+  double* part = (double*)calloc((size_t)nt, sizeof(double));
+  hlbl_qed_params qp;
+  hlbl_qed_params_init(&qp, lambda);
+
+  /* ym and the unmapped yv are site-independent (cuda_lattice.cu:411-416) */
+  double ym[4];
+  for (int r = 0; r < 4; ++r)
+    ym[r] = oracle_coord_map(oracle_mod_pos(yv[r], global[r]), global[r]) * xunit;
+
+#pragma omp parallel
+  {
+    double* corr_I = (double*)malloc(sizeof(double) * 384 * 2);
+    double* corr_II = corr_I + 384;
+    double sum = 0.0;
+#pragma omp for schedule(static)
+    for (long long ix = 0; ix < (long long)V; ++ix) {
+      int coord[4], xv[4], xvzh[4], x_rel[4];
+      site_coords((size_t)ix, local, coord);
+      for (int r = 0; r < 4; ++r) {
+        int xr = coord[r] + pc[r] * local[r] - gsx[r];
+        xr = (xr + global[r]) % global[r];
+        x_rel[r] = xr;
+        xv[r] = oracle_coord_map(xr, global[r]);
+        xvzh[r] = oracle_coord_map_zerohalf(xr, global[r]);
+      }
+      for (int mu = 0; mu < 4; ++mu) {
+        /* dxu[ib][ia] = -conj(g5 g_mu fwd_src[1-f][ia]) . fwd_y[f][ib] (:323-345) */
+        double dxu[12 * 12 * 2];
+        memset(dxu, 0, sizeof dxu);
+        for (int ia = 0; ia < 12; ++ia) {
+          const double* d = fwd_src + ((size_t)((1 - iflavor) * 12 + ia) * V + (size_t)ix) * 24;
+          double t[24];
+          apply_gamma(mu, d, t);
+          times_g5(t);
+          for (int ib = 0; ib < 12; ++ib) {
+            const double* u = fwd_y + ((size_t)(iflavor * 12 + ib) * V + (size_t)ix) * 24;
+            for (int i = 0; i < 12; ++i) {
+              double const tr = t[2 * i], ti = t[2 * i + 1];
+              double const ur = u[2 * i], ui = u[2 * i + 1];
+              dxu[(ib * 12 + ia) * 2] += -(tr * ur + ti * ui);
+              dxu[(ib * 12 + ia) * 2 + 1] += -(tr * ui - ti * ur);
+            }
+          }
+        }
+        /* g_dxu[lambda][ia] = g_lambda g5 dxu[ia] (:379-382, hoisted out of k, nu) */
+        double g_dxu[4][12][24];
+        for (int lam = 0; lam < 4; ++lam)
+          for (int ia = 0; ia < 12; ++ia) {
+            double t[24];
+            apply_gamma(5, dxu + ia * 24, t);
+            apply_gamma(lam, t, g_dxu[lam][ia]);
+          }
+        /* corr_I, corr_II (:346-400) */
+        for (int k = 0; k < 6; ++k) {
+          int const rho = comb[k][0], sigma = comb[k][1];
+          for (int nu = 0; nu < 4; ++nu)
+            for (int lam = 0; lam < 4; ++lam) {
+              double cI = 0.0, cII = 0.0;
+              for (int ia = 0; ia < 12; ++ia)
+                for (int ib = 0; ib < 12; ++ib) {
+                  double const u_re = g_dxu[lam][ia][2 * ib], u_im = g_dxu[lam][ia][2 * ib + 1];
+                  double v_re = g_dzu[(((k * 4 + nu) * 12 + ib) * 12 + ia) * 2];
+                  double v_im = g_dzu[(((k * 4 + nu) * 12 + ib) * 12 + ia) * 2 + 1];
+                  cI -= u_re * v_re - u_im * v_im;
+                  v_re = xvzh[rho] * g_dzsu[(((sigma * 4 + nu) * 12 + ib) * 12 + ia) * 2] -
+                         xvzh[sigma] * g_dzsu[(((rho * 4 + nu) * 12 + ib) * 12 + ia) * 2];
+                  v_im = xvzh[rho] * g_dzsu[(((sigma * 4 + nu) * 12 + ib) * 12 + ia) * 2 + 1] -
+                         xvzh[sigma] * g_dzsu[(((rho * 4 + nu) * 12 + ib) * 12 + ia) * 2 + 1];
+                  cII -= u_re * v_re - u_im * v_im;
+                }
+              corr_I[((k * 4 + mu) * 4 + nu) * 4 + lam] = cI;
+              corr_II[((k * 4 + mu) * 4 + nu) * 4 + lam] = cII;
+            }
+        }
+      }
+      /* QED kernel arguments (:403-426) and the three contractions (:428-476) */
+      double xm[4], xm_mi_ym[4];
+      for (int r = 0; r < 4; ++r) {
+        xm[r] = xv[r] * xunit;
+        xm_mi_ym[r] = oracle_coord_map_diff(x_rel[r], yv[r], global[r]) * xunit;
+      }
+      double kerv[6][4][4][4];
+      double dtmp = 0.0;
+      int i;
+      hlbl_qed_kernel(&qp, xm, ym, kerv);
+      i = 0;
+      for (int k = 0; k < 6; k++)
+        for (int mu = 0; mu < 4; mu++)
+          for (int nu = 0; nu < 4; nu++)
+            for (int lam = 0; lam < 4; lam++) dtmp += kerv[k][mu][nu][lam] * corr_I[i++];
+      hlbl_qed_kernel(&qp, ym, xm, kerv);
+      i = 0;
+      for (int k = 0; k < 6; k++)
+        for (int mu = 0; mu < 4; mu++)
+          for (int nu = 0; nu < 4; nu++)
+            for (int lam = 0; lam < 4; lam++) dtmp += kerv[k][nu][mu][lam] * corr_I[i++];
+      hlbl_qed_kernel(&qp, xm, xm_mi_ym, kerv);
+      i = 0;
+      for (int k = 0; k < 6; k++)
+        for (int mu = 0; mu < 4; mu++)
+          for (int nu = 0; nu < 4; nu++)
+            for (int lam = 0; lam < 4; lam++) {
+              dtmp -= kerv[k][lam][nu][mu] * corr_I[i];
+              dtmp += kerv[k][lam][nu][mu] * corr_II[i];
+              i++;
+            }
+      sum += dtmp;
+    }
+    part[thread_id()] = sum;
+    free(corr_I);
+  }
+  double total = 0.0;
+  for (int th = 0; th < nt; ++th) total += part[th];
+  free(part);
+  return total;
+}
+
+/* ---- Contractor::kernel_sum (contract.cpp:104-114), one rank ---------- */
+void oracle_kernel_sum(const double* fwd_src, const double* fwd_y, const int gsx[4],
+                       const int yv[4], double xunit, double lambda, const int global[4],
+                       const int local[4], const int pc[4], double out[2]) {
+  double dzu[1728], dzsu[1152], g_dzu[6912], g_dzsu[4608];
+  for (int f = 0; f < 2; ++f) {
+    memset(dzu, 0, sizeof dzu);
+    memset(dzsu, 0, sizeof dzsu);
+    oracle_dzu_dzsu(dzu, dzsu, fwd_src, fwd_y, f, pc, gsx, global, local);
+    oracle_insert_gammas(dzu, dzsu, g_dzu, g_dzsu);
+    out[f] = oracle_4pt(g_dzu, g_dzsu, fwd_src, fwd_y, f, pc, gsx, xunit, yv, lambda,
+                        global, local);
+  }
+}
+
+/* Pass 1 of one flavour, summed into the caller's buffers, then gamma
+ * insertion: what compute_dzu_dzsu leaves on the device (contract.cpp:33-81). */
+void oracle_g_dzu_dzsu(const double* fwd_src, const double* fwd_y, int iflavor,
+                       const int gsx[4], const int global[4], const int local[4],
+                       const int pc[4], double* dzu, double* dzsu, double* g_dzu,
+                       double* g_dzsu) {
+  memset(dzu, 0, sizeof(double) * 1728);
+  memset(dzsu, 0, sizeof(double) * 1152);
+  oracle_dzu_dzsu(dzu, dzsu, fwd_src, fwd_y, iflavor, pc, gsx, global, local);
+  oracle_insert_gammas(dzu, dzsu, g_dzu, g_dzsu);
+}

@@ -1,0 +1,136 @@
+// ref_capi.cpp -- TEST INFRASTRUCTURE. A C entry layer over the reference's
+// own sources (kernels/cuda_lattice.cu, src/contract.cpp, src/provider.cpp,
+// src/gamma.cpp, src/geometry.cpp, src/schedule.cpp), compiled as a host
+// emulation with the shims in ./shim. It lets the fixture script run the
+// reference's code on small lattices to pin the oracle. Never shipped.
+#include <cstdint>
+#include <stdexcept>
+#include <vector>
+
+#include "hlbl/contract.hpp"
+#include "hlbl/gamma.hpp"
+#include "hlbl/provider.hpp"
+#include "hlbl/schedule.hpp"
+#include "hlbl_kernels/kernels.cuh"
+
+// KQED entry points, served by the stand-in weight
+extern "C" int initialise(struct QED_kernel_temps* t) {
+  hlbl_qed_params_init(&t->p, 0.4);
+  return 0;
+}
+extern "C" int free_QED_temps(struct QED_kernel_temps*) { return 0; }
+extern "C" void QED_Mkernel_L2(const double Lambda, const double xv[4], const double yv[4],
+                               const struct QED_kernel_temps t, double kerv[6][4][4][4]) {
+  hlbl_qed_params p = t.p;
+  p.lambda = Lambda;
+  hlbl_qed_kernel(&p, xv, yv, kerv);
+}
+
+// contract.cpp links compute_2p2_gpu (2+2 pieces, not emulated here)
+__host__ void compute_2p2_gpu(double*, double*, double*, int const, int const[4], const int*,
+                              int const, const double[2], QED_kernel_temps, unsigned const,
+                              int const[4], MPI_Comm, unsigned const, unsigned const,
+                              unsigned const, unsigned const, unsigned const, unsigned const,
+                              unsigned const, unsigned const) {
+  throw std::runtime_error("compute_2p2_gpu is not part of the host emulation");
+}
+
+namespace {
+Coord coord(const int v[4]) { return Coord{v[0], v[1], v[2], v[3]}; }
+Geom geom(const int v[4]) { return Geom{v[0], v[1], v[2], v[3]}; }
+}  // namespace
+
+extern "C" {
+
+// Contractor::kernel_sum on one rank with lattice `local` (= global).
+int ref_kernel_sum(const int local[4], const double* src, const double* y, const int gsx[4],
+                   const int yv[4], double xunit, double out[2]) {
+  try {
+    hlbl::Lattice lat(MPI_COMM_WORLD, hlbl::Vec4{1, 1, 1, 1},
+                      hlbl::Vec4{local[0], local[1], local[2], local[3]});
+    QED_kernel_temps kq;
+    initialise(&kq);
+    std::size_t const n = hlbl::block_length(lat);
+    hlbl::DeviceBuffer<double> d_src(n), d_y(n);
+    d_src.copy_from_host(src, n);
+    d_y.copy_from_host(y, n);
+    hlbl::Contractor c(lat, kq);
+    auto r = c.kernel_sum(d_src.get(), d_y.get(), hlbl::Vec4{gsx[0], gsx[1], gsx[2], gsx[3]},
+                          hlbl::Vec4{yv[0], yv[1], yv[2], yv[3]}, xunit);
+    out[0] = r[0];
+    out[1] = r[1];
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+// cu_dzu_dzsu with an arbitrary rank position (adds into dzu, dzsu).
+void ref_dzu_dzsu(double* dzu, double* dzsu, const double* src, const double* y, int f,
+                  const int pc[4], const int gsx[4], const int global[4], const int local[4]) {
+  cu_dzu_dzsu(dzu, dzsu, src, y, f, coord(pc), coord(gsx), geom(global), geom(local));
+}
+
+// cu_4pt_contraction with an arbitrary rank position (adds into *ks).
+void ref_4pt(double* ks, const double* g_dzu, const double* g_dzsu, const double* src,
+             const double* y, int f, const int pc[4], const int gsx[4], double xunit,
+             const int yv[4], const int global[4], const int local[4]) {
+  QED_kernel_temps kq;
+  initialise(&kq);
+  cu_4pt_contraction(ks, g_dzu, g_dzsu, src, y, f, coord(pc), coord(gsx), Pair{xunit, 0.0},
+                     coord(yv), kq, geom(global), geom(local));
+}
+
+void ref_fill_random_block(const int local[4], std::uint64_t seed, double* out) {
+  hlbl::Lattice lat(MPI_COMM_WORLD, hlbl::Vec4{1, 1, 1, 1},
+                    hlbl::Vec4{local[0], local[1], local[2], local[3]});
+  hlbl::fill_random_block(lat, seed, out);
+}
+
+// RandomProvider::compute: the block of the source at gsx.
+void ref_random_provider(const int local[4], std::uint64_t seed, const int gsx[4], double* out) {
+  hlbl::Lattice lat(MPI_COMM_WORLD, hlbl::Vec4{1, 1, 1, 1},
+                    hlbl::Vec4{local[0], local[1], local[2], local[3]});
+  hlbl::RandomProvider prov(lat, seed);
+  hlbl::DeviceBuffer<double> d(hlbl::block_length(lat));
+  prov.compute(hlbl::Vec4{gsx[0], gsx[1], gsx[2], gsx[3]}, d);
+  d.copy_to_host(out, hlbl::block_length(lat));
+}
+
+void ref_apply_gamma(int g, const double* in, double* out) {
+  hlbl::Spinor24 t;
+  for (int i = 0; i < 24; ++i) t[i] = in[i];
+  hlbl::Spinor24 s = hlbl::apply_gamma(g, t);
+  for (int i = 0; i < 24; ++i) out[i] = s[i];
+}
+
+// build_schedule + all_pairs: rows (older[4], newer[4], window). Returns the
+// number of pairs, or -1 if max_pairs is too small.
+int ref_schedule_pairs(const int h[4], int stride, int n_steps, const int origin[4], int* out,
+                       int max_pairs) {
+  auto steps = hlbl::build_schedule(hlbl::Vec4{h[0], h[1], h[2], h[3]}, stride, n_steps,
+                                    hlbl::Vec4{origin[0], origin[1], origin[2], origin[3]});
+  int n = 0;
+  for (const auto& st : steps)
+    for (const auto& src : st.sources)
+      for (const auto& q : src.partners) {
+        if (n >= max_pairs) return -1;
+        int* r = out + 9 * n;
+        for (int i = 0; i < 4; ++i) r[i] = q[i];
+        for (int i = 0; i < 4; ++i) r[4 + i] = src.position[i];
+        r[8] = st.index;
+        ++n;
+      }
+  return n;
+}
+
+// simulate(kInterleaved): propagators, pairs, peak cache.
+void ref_schedule_stats(const int h[4], int stride, int n_steps, long long out[3]) {
+  auto steps = hlbl::build_schedule(hlbl::Vec4{h[0], h[1], h[2], h[3]}, stride, n_steps);
+  auto st = hlbl::simulate(steps, hlbl::Mode::kInterleaved);
+  out[0] = st.n_propagators;
+  out[1] = st.n_pairs;
+  out[2] = st.peak_cache;
+}
+
+}  // extern "C"

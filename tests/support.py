@@ -1,0 +1,129 @@
+"""Test helpers: the CPU oracle (oracle/hlbl_oracle.c) through ctypes, and the
+golden fixtures of tests/golden. Test infrastructure only."""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden", "reference_host_emulation.json")
+I4 = C.c_int * 4
+
+
+def i4(v):
+    return I4(*[int(a) for a in v])
+
+
+def vp(a: np.ndarray):
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def volume(v) -> int:
+    return int(v[0]) * int(v[1]) * int(v[2]) * int(v[3])
+
+
+def block_len(v) -> int:
+    return 2 * 12 * 24 * volume(v)
+
+
+_oracle = None
+
+
+def oracle():
+    """The oracle library, built on demand."""
+    global _oracle
+    if _oracle is None:
+        from hlbl_gb300.build import build_oracle
+
+        lib = C.CDLL(build_oracle())
+        vpt, dp = C.c_void_p, C.c_double
+        lib.oracle_fill_random_block.argtypes = [I4, I4, C.c_uint64, vpt]
+        lib.oracle_fill_gaussian_block.argtypes = [I4, I4, C.c_uint64, vpt]
+        lib.oracle_source_seed.restype = C.c_uint64
+        lib.oracle_source_seed.argtypes = [C.c_uint64, I4]
+        lib.oracle_kernel_sum.argtypes = [vpt, vpt, I4, I4, dp, dp, I4, I4, I4, vpt]
+        lib.oracle_dzu_dzsu.argtypes = [vpt, vpt, vpt, vpt, C.c_int, I4, I4, I4, I4]
+        lib.oracle_insert_gammas.argtypes = [vpt, vpt, vpt, vpt]
+        lib.oracle_4pt.restype = dp
+        lib.oracle_4pt.argtypes = [vpt, vpt, vpt, vpt, C.c_int, I4, I4, dp, I4, dp, I4, I4]
+        lib.oracle_apply_gamma.argtypes = [C.c_int, vpt, vpt]
+        lib.oracle_qed_kernel.argtypes = [dp, vpt, vpt, vpt]
+        lib.oracle_qed_weights.argtypes = [dp, dp, dp, dp, vpt]
+        lib.oracle_coord_map.argtypes = [C.c_int, C.c_int]
+        lib.oracle_coord_map_zerohalf.argtypes = [C.c_int, C.c_int]
+        lib.oracle_coord_map_diff.argtypes = [C.c_int, C.c_int, C.c_int]
+        lib.oracle_set_threads.argtypes = [C.c_int]
+        lib.oracle_get_threads.restype = C.c_int
+        _oracle = lib
+    return _oracle
+
+
+def random_block(local, seed, pc=(0, 0, 0, 0)) -> np.ndarray:
+    """fill_random_block (src/provider.cpp:25-57) via the oracle."""
+    out = np.zeros(block_len(local))
+    oracle().oracle_fill_random_block(i4(local), i4(pc), C.c_uint64(seed), vp(out))
+    return out
+
+
+def gaussian_block(local, seed, pc=(0, 0, 0, 0)) -> np.ndarray:
+    out = np.zeros(block_len(local))
+    oracle().oracle_fill_gaussian_block(i4(local), i4(pc), C.c_uint64(seed), vp(out))
+    return out
+
+
+def source_seed(run_seed, gsx) -> int:
+    return int(oracle().oracle_source_seed(C.c_uint64(run_seed), i4(gsx)))
+
+
+def oracle_kernel_sum(src, y, gsx, yv, xunit, lattice, lam=0.4, local=None, pc=(0, 0, 0, 0)):
+    local = lattice if local is None else local
+    out = np.zeros(2)
+    oracle().oracle_kernel_sum(vp(src), vp(y), i4(gsx), i4(yv), C.c_double(xunit),
+                               C.c_double(lam), i4(lattice), i4(local), i4(pc), vp(out))
+    return out
+
+
+def oracle_dz(src, y, f, gsx, lattice, local=None, pc=(0, 0, 0, 0)):
+    local = lattice if local is None else local
+    dzu, dzsu = np.zeros(1728), np.zeros(1152)
+    oracle().oracle_dzu_dzsu(vp(dzu), vp(dzsu), vp(src), vp(y), int(f), i4(pc), i4(gsx),
+                             i4(lattice), i4(local))
+    return dzu, dzsu
+
+
+def oracle_gammas(dzu, dzsu):
+    g_dzu, g_dzsu = np.zeros(6912), np.zeros(4608)
+    oracle().oracle_insert_gammas(vp(np.ascontiguousarray(dzu)), vp(np.ascontiguousarray(dzsu)),
+                                  vp(g_dzu), vp(g_dzsu))
+    return g_dzu, g_dzsu
+
+
+def oracle_4pt(g_dzu, g_dzsu, src, y, f, gsx, xunit, yv, lattice, local=None, pc=(0, 0, 0, 0),
+               lam=0.4):
+    local = lattice if local is None else local
+    return float(oracle().oracle_4pt(vp(g_dzu), vp(g_dzsu), vp(src), vp(y), int(f), i4(pc),
+                                     i4(gsx), C.c_double(xunit), i4(yv), C.c_double(lam),
+                                     i4(lattice), i4(local)))
+
+
+def golden() -> dict:
+    with open(GOLDEN) as fh:
+        return json.load(fh)
+
+
+def case_inputs(case):
+    """The two blocks of a golden kernel-sum case, regenerated bit-exactly."""
+    lat, spec = case["lattice"], case["input"]
+    if spec[0] == "seeds":
+        return random_block(lat, spec[1]), random_block(lat, spec[2])
+    _, seed, gx, gy = spec
+    return random_block(lat, source_seed(seed, gx)), random_block(lat, source_seed(seed, gy))
+
+
+def rel_err(a, b) -> float:
+    a, b = np.asarray(a, dtype=float), np.asarray(b, dtype=float)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
