@@ -1,0 +1,434 @@
+#!/usr/bin/env python
+"""Benchmark: connected-HLbL kernel sums (pairs/s) at 24^3 x 48 on GB300.
+
+Workload (the reference's 24^3 x 48 configuration): lattice T=48, L=24
+(V = 663,552 sites, 3.06 GB per propagator block), i.i.d. complex Gaussian
+FP64 propagator blocks (seeded, generated on the device), the sliding-
+hypercube schedule with stride 2, h = (+1,-1,+1,-1), K = 4 (76 propagators,
+275 pairs). One step = every pair one newly solved source closes (the
+sources of window 1 in solve order: up to 8 pairs each, 65 per window).
+
+Printed (one JSON line, rank 0):
+  value      pairs/s of the fastest exact-to-1e-4 path (FP32 per-site
+             products, FP64 sums) over K steps with the blocks resident in
+             HBM (inputs are 3 GB each, far above the 129 MB L2, so no flush
+             is needed between steps);
+  fp64       pairs/s of the plain FP64 path on the same pairs;
+  e2e        the same metric through the C ABI with host buffers: each step
+             copies its new block from pinned host memory and reads back its
+             kernel sums;
+  roofline   the pass-2 kernel (the dominant one) against measured HBM
+             bandwidth, plus its FLOP rate against the measured FMA peak;
+  cpu_baseline  the CPU oracle (the reference's loops restated in C, plain
+             summation, all host threads) on a bounded sample: a slab of
+             time slices of one pair, scaled to the full volume.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LATTICE = (48, 24, 24, 24)
+STRIDE, H, NSTEPS = 2, (1, -1, 1, -1), 4
+RUN_SEED = 20261203
+MUON_MEV, SPACING_FM = 105.658, 0.1
+BYTES_PER_SITE_PASS = 2 * 2 * 12 * 24 * 8  # two blocks, both flavours, per pass
+METRIC = "pairs/sec & HBM GB/s at 24^3x48: batched+surrogate vs plain FP64 at 1e-4 rel"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def volume(lat):
+    return lat[0] * lat[1] * lat[2] * lat[3]
+
+
+def window_steps():
+    """(new source, [partners]) of windows >= 1, in solve order."""
+    from hlbl_gb300 import schedule
+
+    st = schedule.build_schedule(H, STRIDE, NSTEPS)
+    return [(s.position, list(s.partners)) for w in st[1:] for s in w.sources if s.partners]
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def load_traffic():
+    """Per-launch DRAM bytes of the pass-2 kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "p2_kernel_traffic.json")) as fh:
+            return json.load(fh)
+    except OSError:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm, mx, reasons = [], None, set()
+        for r in rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+                for n, v in zip(names, r[3:7]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle on a slab of time slices of one pair
+# ---------------------------------------------------------------------------
+def cpu_pair_seconds(src_h, y_h, gsx, yv, xu, n_slices, threads=None):
+    """Seconds per pair from a slab sample: pass 1 + pass 2, both flavours,
+    over n_slices time slices, scaled by T / n_slices."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+    import support as S
+
+    o = S.oracle()
+    if threads:
+        o.oracle_set_threads(threads)
+    o.oracle_set_compensated(0)  # the reference's plain loops
+    T, L = LATTICE[0], LATTICE[1:]
+    V = volume(LATTICE)
+    vs = n_slices * L[0] * L[1] * L[2]
+    sl_src = np.ascontiguousarray(src_h.reshape(24, V, 24)[:, :vs, :])
+    sl_y = np.ascontiguousarray(y_h.reshape(24, V, 24)[:, :vs, :])
+    local = (n_slices,) + L
+    t0 = time.perf_counter()
+    for f in (0, 1):
+        dzu, dzsu = S.oracle_dz(sl_src, sl_y, f, gsx, LATTICE, local)
+        g_dzu, g_dzsu = S.oracle_gammas(dzu, dzsu)
+        S.oracle_4pt(g_dzu, g_dzsu, sl_src, sl_y, f, gsx, xu, yv, LATTICE, local)
+    dt = time.perf_counter() - t0
+    o.oracle_set_compensated(1)
+    return dt * T / n_slices, int(o.oracle_get_threads())
+
+
+def pick_slices(src_h, y_h, gsx, yv, xu, budget_s):
+    t1, _ = cpu_pair_seconds(src_h, y_h, gsx, yv, xu, 1)
+    per_slice = t1 / LATTICE[0]
+    return max(1, min(LATTICE[0], int(round(budget_s / max(per_slice, 1e-6)))))
+
+
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    import torch
+
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import hlbl_gb300 as hg
+    from hlbl_gb300 import schedule
+    from hlbl_gb300.contract import measure_fma_peak
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    xu = hg.xunit(MUON_MEV, SPACING_FM)
+    steps_all = window_steps()
+    nst = len(steps_all)
+    # weak scaling: rank r takes steps r, r+world, ... (pairs are independent)
+    order = [steps_all[(rank + world * i) % nst] for i in range(args.warmup + args.steps)]
+    warm, timed = order[:args.warmup], order[args.warmup:]
+
+    c = hg.Contractor(LATTICE, device=local_rank)
+    stream = torch.cuda.Stream()
+    c.set_stream(stream)
+    blocks = {}
+
+    def block(p):
+        site = schedule.mod_pos(p, LATTICE)
+        if site not in blocks:
+            t = torch.empty(c.block_length, dtype=torch.float64, device="cuda")
+            with torch.cuda.stream(stream):
+                c.fill_gaussian_block(t, hg.Contractor.source_seed(RUN_SEED, site))
+            blocks[site] = t
+        return blocks[site]
+
+    for p, qs in order:
+        block(p)
+        for q in qs:
+            block(q)
+    stream.synchronize()
+
+    def pairs_of(step):
+        p, qs = step
+        return [(q, p, schedule.mod_pos(q, LATTICE), schedule.site_map_diff(p, q, LATTICE)) for q in qs]
+
+    n_timed_pairs = sum(len(s[1]) for s in timed)
+    res = torch.zeros((max(1, n_timed_pairs), 2), dtype=torch.float64, device="cuda")
+
+    def run_steps(steps, prec, out=None):
+        k = 0
+        for st in steps:
+            for q, p, gx, yv in pairs_of(st):
+                dst = out[k] if out is not None else res[0]
+                c.kernel_sum_async(block(q), block(p), gx, yv, xu, dst, precision=prec)
+                k += 1
+        return k
+
+    def timed_run(steps, prec, out):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        n = run_steps(steps, prec, out)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return n, ms
+
+    # ---- headline: FP32 products, FP64 sums -------------------------------
+    run_steps(warm, hg.FP32)
+    stream.synchronize()
+    clocks = ClockSampler(local_rank)
+    n32, ms32 = timed_run(timed, hg.FP32, res)
+    clk = clocks.stop()
+    res32 = res.clone()
+
+    # ---- plain FP64 on the first fp64-steps timed steps ---------------------
+    f64_steps = timed[:max(1, args.fp64_steps)]
+    res64 = torch.zeros_like(res)
+    run_steps(warm[:1], hg.FP64)
+    n64, ms64 = timed_run(f64_steps, hg.FP64, res64)
+    a32 = res32[:n64].cpu()
+    a64 = res64[:n64].cpu()
+    rel = ((a32 - a64).abs() / a64.abs().clamp_min(1e-300)).max().item()
+
+    # ---- per-kernel durations (CUDA events on the launching stream) --------
+    c.set_profiling(True)
+    run_steps(timed[:1], hg.FP32)
+    stream.synchronize()
+    (p1ms, p1n), (p2ms, p2n) = c.kernel_times()
+    c.set_profiling(False)
+    c.set_profiling(True)
+    run_steps([(timed[0][0], timed[0][1][:1])], hg.FP64)
+    stream.synchronize()
+    (p1ms64, p1n64), (p2ms64, p2n64) = c.kernel_times()
+    c.set_profiling(False)
+
+    # ---- end to end through the C ABI with host buffers --------------------
+    pinned = {}
+    for p, _ in timed:
+        site = schedule.mod_pos(p, LATTICE)
+        if site not in pinned:
+            h = torch.empty(c.block_length, dtype=torch.float64, pin_memory=True)
+            h.copy_(block(p))
+            pinned[site] = h
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    h2d = d2h = 0
+    for p, qs in timed:
+        site = schedule.mod_pos(p, LATTICE)
+        with torch.cuda.stream(stream):
+            block(p).copy_(pinned[site], non_blocking=True)
+        h2d += pinned[site].numel() * 8
+        for q, pp, gx, yv in pairs_of((p, qs)):
+            c.kernel_sum(block(q), block(pp), gx, yv, xu, hg.FP32)  # blocking, result on host
+            d2h += 16
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    # ---- peaks and roofline -----------------------------------------------
+    peaks, peak_src = load_peaks()
+    fp64_peak = measure_fma_peak(hg.FP64, local_rank)
+    fp32_peak = measure_fma_peak(hg.FP32, local_rank)
+    V = volume(LATTICE)
+    p2_avg_ms = p2ms / max(1, p2n)
+    p1_avg_ms = p1ms / max(1, p1n)
+    bytes_launch = BYTES_PER_SITE_PASS * V
+    achieved = bytes_launch / (p2_avg_ms * 1e-3) / 1e9
+    flop_p2 = 2 * V * 2 * (4 * 288 * 160 + 8 * 144 * 3 * 4 + 640)  # both flavours, FMA = 2 flop
+    traffic = load_traffic()
+
+    pairs_total = n32 * world
+    value = pairs_total / (ms32 * 1e-3)
+    out = {
+        "metric": METRIC,
+        "value": round(value, 4),
+        "unit": "pairs/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms32 / max(1, len(timed)), 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 products, fp64 sums",
+        "data": "synthetic: seeded i.i.d. complex Gaussian FP64 propagator blocks, generated on the device",
+        "config": {"workload": "24^3x48 (T=48,L=24, V=663552), stride 2, h=(+1,-1,+1,-1), K=4; step = "
+                               "the pairs one new source closes (window 1 sources)",
+                   "lattice": list(LATTICE), "pairs_timed": n32, "path": "per-pair FP32 (batched: not yet)",
+                   "qed_weight": "stand-in (KQED unavailable), exact FP64",
+                   "l2": "inputs 3.06 GB per block, larger than L2; no flush"},
+        "fp64": {"value": round(n64 / (ms64 * 1e-3), 4), "unit": "pairs/s", "pairs_timed": n64,
+                 "p2_kernel_ms": round(p2ms64 / max(1, p2n64), 3),
+                 "p1_kernel_ms": round(p1ms64 / max(1, p1n64), 3)},
+        "speedup_vs_fp64": round(value / (n64 / (ms64 * 1e-3)), 2),
+        "max_rel_err_vs_fp64": rel,
+        "e2e": {"value": round(pairs_total / e2e_s, 4), "unit": "pairs/s",
+                "h2d_bytes_per_step": int(h2d / max(1, len(timed))),
+                "d2h_bytes_per_step": int(d2h / max(1, len(timed)))},
+        "roofline": {"bound": "hbm", "kernel": "p2_kernel<float,2,8>",
+                     "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(achieved / peaks["hbm_gbs"], 5),
+                     "traffic": (traffic or {}).get("bytes_per_launch"),
+                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                     "p2_kernel_ms": round(p2_avg_ms, 3), "p1_kernel_ms": round(p1_avg_ms, 3),
+                     "bytes_per_launch": bytes_launch},
+        "compute_roofline": {"bound": "fp32 fma", "achieved_tflops": round(flop_p2 / (p2_avg_ms * 1e-3) / 1e12, 3),
+                             "peak_tflops": round(fp32_peak, 2),
+                             "frac": round(flop_p2 / (p2_avg_ms * 1e-3) / 1e12 / fp32_peak, 4),
+                             "fp64_fma_peak_tflops": round(fp64_peak, 3),
+                             "fp64_p2_tflops": round(flop_p2 / (p2ms64 / max(1, p2n64) * 1e-3) / 1e12, 4),
+                             "peak_source": "measured here (FMA-chain kernel, hlbl_measure_fma_peak)"},
+        "clocks": clk,
+        "gpu_launches": n32 * 6,
+    }
+
+    if rank == 0 and not args.no_cpu_baseline:
+        p, qs = timed[0]
+        q = qs[0]
+        gx = schedule.mod_pos(q, LATTICE)
+        yv = schedule.site_map_diff(p, q, LATTICE)
+        src_h = block(q).cpu().numpy()
+        y_h = block(p).cpu().numpy()
+        ns = pick_slices(src_h, y_h, gx, yv, xu, args.cpu_seconds)
+        sec, cores = cpu_pair_seconds(src_h, y_h, gx, yv, xu, ns)
+        out["cpu_baseline"] = {"value": round(1.0 / sec, 6), "unit": "pairs/s", "cores": cores,
+                               "kind": "port",
+                               "sample": f"one pair, pass 1 + pass 2 both flavours over {ns} of 48 "
+                                         f"time slices, scaled by 48/{ns}; plain FP64 loops of the "
+                                         f"reference restated in C (oracle), OpenMP"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def run_reference(args, rank, world):
+    """The reference arm: the reference's contraction loops on the host cores
+    (the oracle port; the reference has no CPU implementation of its own and
+    its CUDA kernels need KQED), on the same workload, metric and unit."""
+    if rank != 0:
+        return 0
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import support as S
+    from hlbl_gb300 import schedule
+
+    xu = MUON_MEV / 197.3269804 * SPACING_FM
+    steps_all = window_steps()
+    p, qs = steps_all[0]
+    q = qs[0]
+    gx = schedule.mod_pos(q, LATTICE)
+    yv = schedule.site_map_diff(p, q, LATTICE)
+    src_h = S.gaussian_block(LATTICE, S.source_seed(RUN_SEED, schedule.mod_pos(q, LATTICE)))
+    y_h = S.gaussian_block(LATTICE, S.source_seed(RUN_SEED, schedule.mod_pos(p, LATTICE)))
+    budget = max(2.0, 120.0 / max(1, args.steps + args.warmup))
+    ns = pick_slices(src_h, y_h, gx, yv, xu, budget)
+    for _ in range(args.warmup):
+        cpu_pair_seconds(src_h, y_h, gx, yv, xu, 1)
+    secs = []
+    cores = 1
+    for _ in range(args.steps):
+        s, cores = cpu_pair_seconds(src_h, y_h, gx, yv, xu, ns)
+        secs.append(s)
+    sec = statistics.mean(secs)
+    v = 1.0 / sec
+    sample = (f"per step: one pair, pass 1 + pass 2 both flavours over {ns} of 48 time slices, "
+              f"scaled by 48/{ns}")
+    print(json.dumps({
+        "metric": METRIC, "value": round(v, 6), "unit": "pairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3 * ns / 48, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded i.i.d. complex Gaussian FP64 propagator blocks",
+        "config": {"workload": "24^3x48 (T=48,L=24, V=663552), stride 2, h=(+1,-1,+1,-1), K=4",
+                   "lattice": list(LATTICE)},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(v, 6), "unit": "pairs/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(v, 6), "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

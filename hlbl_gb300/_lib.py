@@ -43,6 +43,9 @@ def _load() -> C.CDLL:
         "hlbl_fill_gaussian_block": (C.c_int, [vp, vp, C.c_uint64]),
         "hlbl_source_seed": (C.c_uint64, [C.c_uint64, i4p]),
         "hlbl_block_length": (C.c_size_t, [vp]),
+        "hlbl_ctx_set_profiling": (C.c_int, [vp, C.c_int]),
+        "hlbl_ctx_kernel_times": (C.c_int, [vp, dp, C.POINTER(C.c_longlong)]),
+        "hlbl_measure_fma_peak": (C.c_int, [C.c_int, C.c_int, dp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

@@ -21,6 +21,13 @@ def xunit(muon_mass_mev: float, lattice_spacing_fm: float) -> float:
     return muon_mass_mev / HBARC_MEV_FM * lattice_spacing_fm
 
 
+def measure_fma_peak(precision=FP64, device: int = 0) -> float:
+    """CUDA-core FMA throughput in TFLOP/s (FP64 or FP32)."""
+    out = C.c_double()
+    check(lib.hlbl_measure_fma_peak(int(device), _prec(precision), C.byref(out)))
+    return out.value
+
+
 def _prec(p) -> int:
     if p in (FP64, "fp64"):
         return FP64
@@ -127,6 +134,18 @@ class Contractor:
         """Contractor::pieces_2p2 (contract.cpp:116-156) is not part of this
         library: the 2+2 pieces are a different contraction."""
         raise NotImplementedError("the 2+2 pieces (compute_2p2_gpu) are not implemented here")
+
+    # -- measurement ---------------------------------------------------------
+    def set_profiling(self, on: bool) -> None:
+        """Time every pass-1/pass-2 kernel with CUDA events (resets totals)."""
+        check(lib.hlbl_ctx_set_profiling(self._h, 1 if on else 0))
+
+    def kernel_times(self):
+        """((pass-1 ms, launches), (pass-2 ms, launches)) since profiling began."""
+        ms = (C.c_double * 2)()
+        n = (C.c_longlong * 2)()
+        check(lib.hlbl_ctx_kernel_times(self._h, ms, n))
+        return (ms[0], n[0]), (ms[1], n[1])
 
     # -- fixtures (src/provider.cpp) ---------------------------------------
     def fill_random_block(self, d_out, seed: int) -> None:

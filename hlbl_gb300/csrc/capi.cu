@@ -172,9 +172,38 @@ struct hlbl_ctx {
   void* d_bt = nullptr;       // [2][288*160] of double (float uses half of it)
   double* d_out = nullptr;    // [2]
   double* h_out = nullptr;    // pinned [2]
+  // optional per-kernel timing with CUDA events on the launching stream
+  bool profiling = false;
+  cudaEvent_t ev[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [pass][begin/end]
+  double prof_ms[2] = {0, 0};
+  long long prof_n[2] = {0, 0};
+  int prof_pending[2] = {0, 0};
 };
 
 namespace hg {
+
+// Profiling: events around one kernel; the elapsed time is collected at
+// the next prof_begin of that pass (or by hlbl_ctx_kernel_times).
+void prof_collect(hlbl_ctx* c, int pass) {
+  if (!c->profiling || c->prof_pending[pass] == 0) return;
+  float ms = 0.f;
+  if (cudaEventSynchronize(c->ev[pass][1]) == cudaSuccess &&
+      cudaEventElapsedTime(&ms, c->ev[pass][0], c->ev[pass][1]) == cudaSuccess) {
+    c->prof_ms[pass] += ms;
+    c->prof_n[pass] += 1;
+  }
+  c->prof_pending[pass] = 0;
+}
+void prof_begin(hlbl_ctx* c, int pass) {
+  if (!c->profiling) return;
+  prof_collect(c, pass);
+  cudaEventRecord(c->ev[pass][0], c->stream);
+}
+void prof_end(hlbl_ctx* c, int pass) {
+  if (!c->profiling) return;
+  cudaEventRecord(c->ev[pass][1], c->stream);
+  c->prof_pending[pass] = 1;
+}
 
 // Pass 1 + reduction + gamma insertion + Bt for flavours [f0, f0+nf).
 // g_dzu/g_dzsu of flavour fl land at d_g + fl*kGLen (+kGDzuLen).
@@ -183,6 +212,7 @@ int run_pass1(hlbl_ctx* c, const Geometry& geo, const double* src, const double*
               double* add_dzsu, bool build_bt) {
   int4 const g4 = make_int4(gsx[0], gsx[1], gsx[2], gsx[3]);
   int grid;
+  prof_begin(c, 0);
   if (precision == HLBL_FP64) {
     if (nf == 2) { grid = (int)std::min<long long>(c->grid_p1d2, P1D2::tiles(geo.V)); P1D2::launch(grid, c->stream, src, y, geo, g4, f0, c->d_part1); }
     else { grid = (int)std::min<long long>(c->grid_p1d1, P1D1::tiles(geo.V)); P1D1::launch(grid, c->stream, src, y, geo, g4, f0, c->d_part1); }
@@ -190,6 +220,7 @@ int run_pass1(hlbl_ctx* c, const Geometry& geo, const double* src, const double*
     if (nf == 2) { grid = (int)std::min<long long>(c->grid_p1f2, P1F2::tiles(geo.V)); P1F2::launch(grid, c->stream, src, y, geo, g4, f0, c->d_part1); }
     else { grid = (int)std::min<long long>(c->grid_p1f1, P1F1::tiles(geo.V)); P1F1::launch(grid, c->stream, src, y, geo, g4, f0, c->d_part1); }
   }
+  prof_end(c, 0);
   p1_reduce_kernel<<<dim3((kDzLen + 255) / 256, nf), 256, 0, c->stream>>>(c->d_part1, grid, nf, c->d_dz,
                                                                           add_dzu, add_dzsu);
   if (!build_bt) return HLBL_OK;
@@ -214,6 +245,7 @@ int run_pass2(hlbl_ctx* c, const Geometry& geo, const double* src, const double*
   a.f0 = f0;
   a.qp = c->qp;
   int grid;
+  prof_begin(c, 1);
   if (precision == HLBL_FP64) {
     const double* bt = static_cast<const double*>(c->d_bt);
     if (nf == 2) { grid = (int)std::min<long long>(c->grid_p2d2, P2D2::tiles(geo.V)); P2D2::launch(grid, c->stream, src, y, geo, a, bt, c->d_part2); }
@@ -223,6 +255,7 @@ int run_pass2(hlbl_ctx* c, const Geometry& geo, const double* src, const double*
     if (nf == 2) { grid = (int)std::min<long long>(c->grid_p2f2, P2F2::tiles(geo.V)); P2F2::launch(grid, c->stream, src, y, geo, a, bt, c->d_part2); }
     else { grid = (int)std::min<long long>(c->grid_p2f1, P2F1::tiles(geo.V)); P2F1::launch(grid, c->stream, src, y, geo, a, bt, c->d_part2); }
   }
+  prof_end(c, 1);
   p2_reduce_kernel<<<1, 32, 0, c->stream>>>(c->d_part2, grid, nf, out, add);
   return HLBL_OK;
 }
@@ -299,6 +332,9 @@ void hlbl_ctx_destroy(hlbl_ctx* c) {
   cudaFree(c->d_bt);
   cudaFree(c->d_out);
   if (c->h_out) cudaFreeHost(c->h_out);
+  for (auto& pe : c->ev)
+    for (auto& e : pe)
+      if (e) cudaEventDestroy(e);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
 }
@@ -406,6 +442,30 @@ int hlbl_reserve_kernel_memory(hlbl_ctx* c, size_t* bytes) {
   e = cudaMemGetInfo(&free1, &total);
   if (e != cudaSuccess) return cuda_fail(e, "hlbl_reserve_kernel_memory");
   *bytes = free0 > free1 ? free0 - free1 : 0;
+  return HLBL_OK;
+}
+
+int hlbl_ctx_set_profiling(hlbl_ctx* c, int on) {
+  if (!c) return fail(HLBL_EINVAL, "hlbl_ctx_set_profiling: null context");
+  if (on && !c->ev[0][0]) {
+    for (auto& pe : c->ev)
+      for (auto& e : pe) {
+        cudaError_t er = cudaEventCreate(&e);
+        if (er != cudaSuccess) return cuda_fail(er, "cudaEventCreate");
+      }
+  }
+  c->profiling = on != 0;
+  c->prof_ms[0] = c->prof_ms[1] = 0;
+  c->prof_n[0] = c->prof_n[1] = 0;
+  c->prof_pending[0] = c->prof_pending[1] = 0;
+  return HLBL_OK;
+}
+
+int hlbl_ctx_kernel_times(hlbl_ctx* c, double ms[2], long long n[2]) {
+  if (!c || !ms || !n) return fail(HLBL_EINVAL, "hlbl_ctx_kernel_times: null argument");
+  prof_collect(c, 0);
+  prof_collect(c, 1);
+  for (int p = 0; p < 2; ++p) { ms[p] = c->prof_ms[p]; n[p] = c->prof_n[p]; }
   return HLBL_OK;
 }
 

@@ -21,6 +21,17 @@ constexpr int kGDzuLen = 6912;
 constexpr int kBtK = 288;          // rows of Bt: (p, q, re/im)
 constexpr int kBtN = 160;          // columns of Bt: (j, nu, lambda), j < 10
 
+// Neumaier's compensated FP64 sum: the site-block and volume sums.
+struct Neu {
+  double s = 0.0, c = 0.0;
+  __device__ __forceinline__ void add(double v) {
+    double const t = s + v;
+    c += fabs(s) >= fabs(v) ? (s - t) + v : (v - t) + s;
+    s = t;
+  }
+  __device__ __forceinline__ double get() const { return s + c; }
+};
+
 // ---------------------------------------------------------------------------
 // Tile loader: rows (which, fl, ia) of the two blocks into shared memory as T.
 // which = 0 reads `a` at flavour fa(fl), which = 1 reads `b` at fb(fl).
@@ -72,11 +83,10 @@ p1_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry
   int const t = threadIdx.x;
   int const fl = t / 144, ia = (t % 144) / 12, ib = t % 12;
 
-  double acc_u[6][2], acc_s[4][2];
-#pragma unroll
-  for (int k = 0; k < 6; ++k) acc_u[k][0] = acc_u[k][1] = 0.0;
-#pragma unroll
-  for (int s = 0; s < 4; ++s) acc_s[s][0] = acc_s[s][1] = 0.0;
+  // FP64 per-thread sums over this CTA's tiles: compensated on the FP64
+  // path, plain on the FP32 path (whose tile sums are only FP32-accurate).
+  constexpr bool kComp = sizeof(T) == sizeof(double);
+  Neu acc_u[6][2], acc_s[4][2];
 
   long long const ntiles = (geo.V + TS - 1) / TS;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -146,21 +156,31 @@ p1_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry
       }
     }
 #pragma unroll
-    for (int k = 0; k < 6; ++k) { acc_u[k][0] += (double)tu[k][0]; acc_u[k][1] += (double)tu[k][1]; }
+    for (int k = 0; k < 6; ++k)
 #pragma unroll
-    for (int s = 0; s < 4; ++s) { acc_s[s][0] += (double)ts[s][0]; acc_s[s][1] += (double)ts[s][1]; }
+      for (int e = 0; e < 2; ++e) {
+        if (kComp) acc_u[k][e].add((double)tu[k][e]);
+        else acc_u[k][e].s += (double)tu[k][e];
+      }
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        if (kComp) acc_s[s][e].add((double)ts[s][e]);
+        else acc_s[s][e].s += (double)ts[s][e];
+      }
   }
 
   double* out = partials + ((size_t)blockIdx.x * NF + fl) * kDzLen;
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
-    out[((k * 12 + ia) * 12 + ib) * 2] = acc_u[k][0];
-    out[((k * 12 + ia) * 12 + ib) * 2 + 1] = acc_u[k][1];
+    out[((k * 12 + ia) * 12 + ib) * 2] = acc_u[k][0].get();
+    out[((k * 12 + ia) * 12 + ib) * 2 + 1] = acc_u[k][1].get();
   }
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
-    out[kDzuLen + ((s * 12 + ia) * 12 + ib) * 2] = acc_s[s][0];
-    out[kDzuLen + ((s * 12 + ia) * 12 + ib) * 2 + 1] = acc_s[s][1];
+    out[kDzuLen + ((s * 12 + ia) * 12 + ib) * 2] = acc_s[s][0].get();
+    out[kDzuLen + ((s * 12 + ia) * 12 + ib) * 2 + 1] = acc_s[s][1].get();
   }
 }
 
@@ -289,7 +309,7 @@ p2_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry
 #pragma unroll
   for (int r = 0; r < 4; ++r) ym[r] = coord_map(mod_pos(args.yv[r], geo.global[r]), geo.global[r]) * xu;
 
-  double run = 0.0;  // this thread's FP64 running sum for its flavour
+  Neu run;  // this thread's compensated FP64 running sum for its flavour
   long long const ntiles = (geo.V + TS - 1) / TS;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     long long const s0 = tile * TS;
@@ -424,23 +444,30 @@ p2_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry
       for (int s = 0; s < TS; ++s)
 #pragma unroll
         for (int mu = 0; mu < 4; ++mu) part += s_coef[(s * 4 + mu) * kBtN + n] * acc[s][mu];
-      run -= (double)part;
+      run.add(-(double)part);
     }
   }
 
   // block reduction per flavour in a fixed order: warp shuffles, then warps
-  __shared__ double s_red[32];
-  double v = run;
+  // (a compensated tree: each level adds the pair's sums and their
+  // rounding errors; the error terms travel with them)
+  __shared__ double s_red[32][2];
+  Neu v = run;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  for (int o = 16; o > 0; o >>= 1) {
+    double const os = __shfl_down_sync(0xffffffffu, v.s, o);
+    double const oc = __shfl_down_sync(0xffffffffu, v.c, o);
+    v.add(os);
+    v.c += oc;
+  }
   __syncthreads();
-  if ((t & 31) == 0) s_red[t >> 5] = v;
+  if ((t & 31) == 0) { s_red[t >> 5][0] = v.s; s_red[t >> 5][1] = v.c; }
   __syncthreads();
   if (t < NF) {
     // warps [fl*160/32, (fl+1)*160/32) hold flavour fl (160 = 5 warps)
-    double s = 0.0;
-    for (int w = t * (kBtN / 32); w < (t + 1) * (kBtN / 32); ++w) s += s_red[w];
-    partials[(size_t)blockIdx.x * NF + t] = s;
+    Neu s;
+    for (int w = t * (kBtN / 32); w < (t + 1) * (kBtN / 32); ++w) { s.add(s_red[w][0]); s.c += s_red[w][1]; }
+    partials[(size_t)blockIdx.x * NF + t] = s.get();
   }
 }
 

@@ -107,6 +107,16 @@ int hlbl_fill_random_block(hlbl_ctx* ctx, double* d_out, uint64_t seed);
 int hlbl_fill_gaussian_block(hlbl_ctx* ctx, double* d_out, uint64_t seed);
 uint64_t hlbl_source_seed(uint64_t run_seed, const int gsx[4]);
 
+/* Measurement hooks. With profiling on, the context times every pass-1 and
+ * pass-2 contraction kernel with CUDA events on its launching stream;
+ * hlbl_ctx_kernel_times returns the summed milliseconds and launch counts
+ * ([0] pass 1, [1] pass 2) since profiling was switched on. */
+int hlbl_ctx_set_profiling(hlbl_ctx* ctx, int on);
+int hlbl_ctx_kernel_times(hlbl_ctx* ctx, double ms[2], long long n[2]);
+/* FMA throughput of the CUDA cores (TFLOP/s, precision HLBL_FP64 or
+ * HLBL_FP32), from a kernel of independent FMA chains. */
+int hlbl_measure_fma_peak(int device, int precision, double* tflops);
+
 /* Device doubles in one propagator block of this rank. */
 size_t hlbl_block_length(const hlbl_ctx* ctx);
 

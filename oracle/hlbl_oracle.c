@@ -95,6 +95,24 @@ static int thread_id(void) {
 #endif
 }
 
+/* Summation mode. Compensated (the default, used as the checker): every sum
+ * over sites, the 144-term corr sums and the 1536-term per-site sum use
+ * Neumaier's compensated summation, which removes the order dependence the
+ * reference's plain loops have on sums that nearly cancel. Plain: the
+ * reference's own plain accumulation, used to time the CPU baseline. */
+static int g_compensated = 1;
+void oracle_set_compensated(int on) { g_compensated = on != 0; }
+int oracle_get_compensated(void) { return g_compensated; }
+
+typedef struct { double s, c; } acc_t;
+static inline void acc_add(acc_t* a, double v) {
+  if (!g_compensated) { a->s += v; return; }
+  double const t = a->s + v;
+  a->c += fabs(a->s) >= fabs(v) ? (a->s - t) + v : (v - t) + a->s;
+  a->s = t;
+}
+static inline double acc_get(const acc_t* a) { return a->s + a->c; }
+
 void oracle_set_threads(int n) {
 #ifdef _OPENMP
   if (n > 0) omp_set_num_threads(n);
@@ -183,11 +201,11 @@ void oracle_dzu_dzsu(double* dzu, double* dzsu, const double* fwd_src, const dou
                      const int local[4]) {
   size_t const V = (size_t)local[0] * local[1] * local[2] * local[3];
   int const nt = n_threads();
-  double* part = (double*)calloc((size_t)nt * 2880, sizeof(double));
+  acc_t* part = (acc_t*)calloc((size_t)nt * 2880, sizeof(acc_t));
 #pragma omp parallel
   {
-    double* acc_u = part + (size_t)thread_id() * 2880; /* [6][12][12][2] */
-    double* acc_s = acc_u + 1728;                       /* [4][12][12][2] */
+    acc_t* acc_u = part + (size_t)thread_id() * 2880; /* [6][12][12][2] */
+    acc_t* acc_s = acc_u + 1728;                       /* [4][12][12][2] */
 #pragma omp for schedule(static)
     for (long long iz = 0; iz < (long long)V; ++iz) {
       int coord[4], zf[4];
@@ -218,8 +236,8 @@ void oracle_dzu_dzsu(double* dzu, double* dzsu, const double* fwd_src, const dou
               re += yr * sr + yi * si;
               im += yr * si - yi * sr;
             }
-            acc_u[((k * 12 + ia) * 12 + ib) * 2] += re;
-            acc_u[((k * 12 + ia) * 12 + ib) * 2 + 1] += im;
+            acc_add(&acc_u[((k * 12 + ia) * 12 + ib) * 2], re);
+            acc_add(&acc_u[((k * 12 + ia) * 12 + ib) * 2 + 1], im);
           }
         }
         for (int s = 0; s < 4; ++s) {
@@ -232,16 +250,21 @@ void oracle_dzu_dzsu(double* dzu, double* dzsu, const double* fwd_src, const dou
               re += yr * t[s][2 * i] + yi * t[s][2 * i + 1];
               im += yr * t[s][2 * i + 1] - yi * t[s][2 * i];
             }
-            acc_s[((s * 12 + ia) * 12 + ib) * 2] += re;
-            acc_s[((s * 12 + ia) * 12 + ib) * 2 + 1] += im;
+            acc_add(&acc_s[((s * 12 + ia) * 12 + ib) * 2], re);
+            acc_add(&acc_s[((s * 12 + ia) * 12 + ib) * 2 + 1], im);
           }
         }
       }
     }
   }
-  for (int th = 0; th < nt; ++th) {
-    for (int i = 0; i < 1728; ++i) dzu[i] += part[(size_t)th * 2880 + i];
-    for (int i = 0; i < 1152; ++i) dzsu[i] += part[(size_t)th * 2880 + 1728 + i];
+  for (int i = 0; i < 2880; ++i) {
+    acc_t a = {0.0, 0.0};
+    for (int th = 0; th < nt; ++th) {
+      acc_add(&a, part[(size_t)th * 2880 + i].s);
+      acc_add(&a, part[(size_t)th * 2880 + i].c);
+    }
+    if (i < 1728) dzu[i] += acc_get(&a);
+    else dzsu[i - 1728] += acc_get(&a);
   }
   free(part);
 }
@@ -276,7 +299,7 @@ double oracle_4pt(const double* g_dzu, const double* g_dzsu, const double* fwd_s
                   const int local[4]) {
   size_t const V = (size_t)local[0] * local[1] * local[2] * local[3];
   int const nt = n_threads();
-  double* part = (double*)calloc((size_t)nt, sizeof(double));
+  acc_t* part = (acc_t*)calloc((size_t)nt, sizeof(acc_t));
   hlbl_qed_params qp;
   hlbl_qed_params_init(&qp, lambda);
 
@@ -289,7 +312,7 @@ double oracle_4pt(const double* g_dzu, const double* g_dzsu, const double* fwd_s
   {
     double* corr_I = (double*)malloc(sizeof(double) * 384 * 2);
     double* corr_II = corr_I + 384;
-    double sum = 0.0;
+    acc_t sum = {0.0, 0.0};
 #pragma omp for schedule(static)
     for (long long ix = 0; ix < (long long)V; ++ix) {
       int coord[4], xv[4], xvzh[4], x_rel[4];
@@ -333,21 +356,21 @@ double oracle_4pt(const double* g_dzu, const double* g_dzsu, const double* fwd_s
           int const rho = comb[k][0], sigma = comb[k][1];
           for (int nu = 0; nu < 4; ++nu)
             for (int lam = 0; lam < 4; ++lam) {
-              double cI = 0.0, cII = 0.0;
+              acc_t cI = {0.0, 0.0}, cII = {0.0, 0.0};
               for (int ia = 0; ia < 12; ++ia)
                 for (int ib = 0; ib < 12; ++ib) {
                   double const u_re = g_dxu[lam][ia][2 * ib], u_im = g_dxu[lam][ia][2 * ib + 1];
                   double v_re = g_dzu[(((k * 4 + nu) * 12 + ib) * 12 + ia) * 2];
                   double v_im = g_dzu[(((k * 4 + nu) * 12 + ib) * 12 + ia) * 2 + 1];
-                  cI -= u_re * v_re - u_im * v_im;
+                  acc_add(&cI, -(u_re * v_re - u_im * v_im));
                   v_re = xvzh[rho] * g_dzsu[(((sigma * 4 + nu) * 12 + ib) * 12 + ia) * 2] -
                          xvzh[sigma] * g_dzsu[(((rho * 4 + nu) * 12 + ib) * 12 + ia) * 2];
                   v_im = xvzh[rho] * g_dzsu[(((sigma * 4 + nu) * 12 + ib) * 12 + ia) * 2 + 1] -
                          xvzh[sigma] * g_dzsu[(((rho * 4 + nu) * 12 + ib) * 12 + ia) * 2 + 1];
-                  cII -= u_re * v_re - u_im * v_im;
+                  acc_add(&cII, -(u_re * v_re - u_im * v_im));
                 }
-              corr_I[((k * 4 + mu) * 4 + nu) * 4 + lam] = cI;
-              corr_II[((k * 4 + mu) * 4 + nu) * 4 + lam] = cII;
+              corr_I[((k * 4 + mu) * 4 + nu) * 4 + lam] = acc_get(&cI);
+              corr_II[((k * 4 + mu) * 4 + nu) * 4 + lam] = acc_get(&cII);
             }
         }
       }
@@ -358,39 +381,42 @@ double oracle_4pt(const double* g_dzu, const double* g_dzsu, const double* fwd_s
         xm_mi_ym[r] = oracle_coord_map_diff(x_rel[r], yv[r], global[r]) * xunit;
       }
       double kerv[6][4][4][4];
-      double dtmp = 0.0;
+      acc_t dtmp = {0.0, 0.0};
       int i;
       hlbl_qed_kernel(&qp, xm, ym, kerv);
       i = 0;
       for (int k = 0; k < 6; k++)
         for (int mu = 0; mu < 4; mu++)
           for (int nu = 0; nu < 4; nu++)
-            for (int lam = 0; lam < 4; lam++) dtmp += kerv[k][mu][nu][lam] * corr_I[i++];
+            for (int lam = 0; lam < 4; lam++) acc_add(&dtmp, kerv[k][mu][nu][lam] * corr_I[i++]);
       hlbl_qed_kernel(&qp, ym, xm, kerv);
       i = 0;
       for (int k = 0; k < 6; k++)
         for (int mu = 0; mu < 4; mu++)
           for (int nu = 0; nu < 4; nu++)
-            for (int lam = 0; lam < 4; lam++) dtmp += kerv[k][nu][mu][lam] * corr_I[i++];
+            for (int lam = 0; lam < 4; lam++) acc_add(&dtmp, kerv[k][nu][mu][lam] * corr_I[i++]);
       hlbl_qed_kernel(&qp, xm, xm_mi_ym, kerv);
       i = 0;
       for (int k = 0; k < 6; k++)
         for (int mu = 0; mu < 4; mu++)
           for (int nu = 0; nu < 4; nu++)
             for (int lam = 0; lam < 4; lam++) {
-              dtmp -= kerv[k][lam][nu][mu] * corr_I[i];
-              dtmp += kerv[k][lam][nu][mu] * corr_II[i];
+              acc_add(&dtmp, -(kerv[k][lam][nu][mu] * corr_I[i]));
+              acc_add(&dtmp, kerv[k][lam][nu][mu] * corr_II[i]);
               i++;
             }
-      sum += dtmp;
+      acc_add(&sum, acc_get(&dtmp));
     }
     part[thread_id()] = sum;
     free(corr_I);
   }
-  double total = 0.0;
-  for (int th = 0; th < nt; ++th) total += part[th];
+  acc_t total = {0.0, 0.0};
+  for (int th = 0; th < nt; ++th) {
+    acc_add(&total, part[th].s);
+    acc_add(&total, part[th].c);
+  }
   free(part);
-  return total;
+  return acc_get(&total);
 }
 
 /* ---- Contractor::kernel_sum (contract.cpp:104-114), one rank ---------- */

@@ -58,6 +58,8 @@ def oracle():
         lib.oracle_coord_map_diff.argtypes = [C.c_int, C.c_int, C.c_int]
         lib.oracle_set_threads.argtypes = [C.c_int]
         lib.oracle_get_threads.restype = C.c_int
+        lib.oracle_set_compensated.argtypes = [C.c_int]
+        lib.oracle_get_compensated.restype = C.c_int
         _oracle = lib
     return _oracle
 
