@@ -29,10 +29,14 @@ def measure_fma_peak(precision=FP64, device: int = 0) -> float:
 
 
 def _prec(p) -> int:
-    if p in (FP64, "fp64"):
+    """'fp64'/'fp32' names, or an integer passed to the C ABI as is (which
+    rejects values other than HLBL_FP64/HLBL_FP32 with HLBL_EINVAL)."""
+    if p == "fp64":
         return FP64
-    if p in (FP32, "fp32"):
+    if p == "fp32":
         return FP32
+    if isinstance(p, int):
+        return p
     raise ValueError(f"precision must be fp64 or fp32, not {p!r}")
 
 
