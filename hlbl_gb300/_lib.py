@@ -35,6 +35,7 @@ def _load() -> C.CDLL:
         "hlbl_kernel_sum": (C.c_int, [vp, vp, vp, i4p, i4p, C.c_double, C.c_int, dp]),
         "hlbl_kernel_sum_async": (C.c_int, [vp, vp, vp, i4p, i4p, C.c_double, C.c_int, vp]),
         "hlbl_cu_dzu_dzsu": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, i4p, i4p, i4p, i4p]),
+        "hlbl_cu_dzu_dzsu_noalloc": (C.c_int, [vp, vp, vp, vp, C.c_int, i4p, i4p, i4p, i4p, vp]),
         "hlbl_cu_4pt_contraction": (C.c_int, [vp, vp, vp, vp, vp, vp, C.c_int, i4p, i4p,
                                               C.c_double, i4p, i4p, i4p]),
         "hlbl_insert_gammas": (C.c_int, [vp, vp, vp, vp, vp]),

@@ -187,7 +187,7 @@ p1_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry
 // Fixed-order, compensated (Neumaier) FP64 sum over the CTAs' partials.
 // dz[fl][i] = sum_cta partials[cta][fl][i]; if add_to != null also
 // add_to[fl][i] += dz (the reference's accumulate-into-caller semantics).
-__global__ void p1_reduce_kernel(const double* __restrict__ partials, int ncta, int nf,
+static __global__ void p1_reduce_kernel(const double* __restrict__ partials, int ncta, int nf,
                                  double* __restrict__ dz, double* add_dzu, double* add_dzsu) {
   int const fl = blockIdx.y;
   int const i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -209,7 +209,7 @@ __global__ void p1_reduce_kernel(const double* __restrict__ partials, int ncta, 
 
 // The host gamma insertion of compute_dzu_dzsu (contract.cpp:58-77) on the
 // device: g_dzu[k][mu][ia] = g_mu g5 dzu[k][ia], g_dzsu[s][mu][ia] the same.
-__global__ void g_build_kernel(const double* __restrict__ dz, int nf, double* __restrict__ g) {
+static __global__ void g_build_kernel(const double* __restrict__ dz, int nf, double* __restrict__ g) {
   int const fl = blockIdx.y;
   int const i = blockIdx.x * blockDim.x + threadIdx.x;  // complex index into g
   if (i >= kGLen / 2 || fl >= nf) return;
@@ -289,6 +289,14 @@ template <typename T, int NF, int TS>
 constexpr size_t p1_smem_bytes() {
   return sizeof(T) * (size_t)(2 * NF * 12 * TS * 24) + sizeof(int) * TS * 4;
 }
+
+// The pass-1 variant of hlbl_cu_dzu_dzsu_noalloc: one flavour, FP64, the
+// same tile as the context's FP64 pass 1.
+struct P1NoAllocTraits {
+  static constexpr int kTS = 16;
+  static constexpr int kThreads = 144;
+  static constexpr size_t kSmem = p1_smem_bytes<double, 1, kTS>();
+};
 
 template <typename T, int NF, int TS>
 __global__ void __launch_bounds__(NF * 160)
@@ -473,7 +481,7 @@ p2_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry
 
 // out[fl] = sum_cta partials[cta][fl] (fixed order, compensated); if add
 // is set, out[fl] is added to rather than written.
-__global__ void p2_reduce_kernel(const double* __restrict__ partials, int ncta, int nf,
+static __global__ void p2_reduce_kernel(const double* __restrict__ partials, int ncta, int nf,
                                  double* __restrict__ out, int add) {
   int const fl = threadIdx.x;
   if (fl >= nf) return;

@@ -90,6 +90,26 @@ int hlbl_cu_4pt_contraction(hlbl_ctx* ctx, double* d_kernel_sum, const double* d
                             const int gsx[4], double xunit, const int yv[4],
                             const int global_geom[4], const int local_geom[4]);
 
+/* Pass 1 of one flavour, as hlbl_cu_dzu_dzsu, for callers that cannot
+ * allocate device memory when they contract: for example a process whose
+ * solver has already taken nearly all device memory into its own pool, or
+ * one that measures free memory around the kernels. It needs no context and
+ * allocates nothing. Its scratch (per-thread-block partial sums) is a fixed
+ * array of HLBL_NOALLOC_MAX_BLOCKS x 2880 doubles (11.8 MB) in the library's
+ * device image, held on every GPU that loads the library until exit; a call
+ * whose pass 1 would run more thread blocks than that fails with
+ * HLBL_EINVAL. Runs on `stream` (a cudaStream_t; NULL = legacy default) on
+ * the current device. The first call on a device looks up the array's device
+ * address and the kernel's occupancy, so make that first call before any
+ * stream capture. All calls share the array: calls that overlap on the GPU
+ * (other streams, other host threads) race and give wrong sums; order them.
+ * No counterpart in the reference. */
+#define HLBL_NOALLOC_MAX_BLOCKS 512
+int hlbl_cu_dzu_dzsu_noalloc(double* d_dzu, double* d_dzsu, const double* fwd_src,
+                             const double* fwd_y, int iflavor, const int proc_coords[4],
+                             const int gsx[4], const int global_geom[4],
+                             const int local_geom[4], void* stream);
+
 /* The gamma insertion of Contractor::compute_dzu_dzsu (contract.cpp:58-77)
  * on the device: g_dzu, g_dzsu from dzu, dzsu (one flavour). Asynchronous. */
 int hlbl_insert_gammas(hlbl_ctx* ctx, const double* d_dzu, const double* d_dzsu,
