@@ -57,7 +57,16 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    return ap.parse_args()
+    ap.add_argument("--train-samples", type=int, default=4 * 1024 * 1024)
+    ap.add_argument("--train-steps", type=int, default=12000)
+    ap.add_argument("--lattice", default=None,
+                    help="T,LX,LY,LZ of a smaller lattice (profiling runs); default 48,24,24,24")
+    args = ap.parse_args()
+    if args.lattice:
+        global LATTICE
+        LATTICE = tuple(int(a) for a in args.lattice.split(","))
+        assert len(LATTICE) == 4
+    return args
 
 
 def volume(lat):
@@ -219,24 +228,39 @@ def main():
         return [(q, p, schedule.mod_pos(q, LATTICE), schedule.site_map_diff(p, q, LATTICE)) for q in qs]
 
     n_timed_pairs = sum(len(s[1]) for s in timed)
-    res = torch.zeros((max(1, n_timed_pairs), 2), dtype=torch.float64, device="cuda")
+    n_rows = max(16, n_timed_pairs, sum(len(s[1]) for s in warm))
+    res = torch.zeros((n_rows, 2), dtype=torch.float64, device="cuda")
 
-    def run_steps(steps, prec, out=None):
+    def step_args(st):
+        pr = pairs_of(st)
+        return (block(st[0]), [block(q) for q, _, _, _ in pr], [g for _, _, g, _ in pr],
+                [v for _, _, _, v in pr])
+
+    def run_batched(steps, prec, out):
+        """One batched call per step (the pairs its new source closes)."""
+        k = 0
+        for st in steps:
+            y_b, xs, gs, vs = step_args(st)
+            c.kernel_sums_batched(y_b, xs, gs, vs, xu, out[k:k + len(xs)], prec)
+            k += len(xs)
+        return k
+
+    def run_pairs(steps, prec, out):
+        """The per-pair API, one call per pair (the reference driver's loop)."""
         k = 0
         for st in steps:
             for q, p, gx, yv in pairs_of(st):
-                dst = out[k] if out is not None else res[0]
-                c.kernel_sum_async(block(q), block(p), gx, yv, xu, dst, precision=prec)
+                c.kernel_sum_async(block(q), block(p), gx, yv, xu, out[k], precision=prec)
                 k += 1
         return k
 
-    def timed_run(steps, prec, out):
+    def timeit(fn, *a):
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
         ev0.record(stream)
-        n = run_steps(steps, prec, out)
+        n = fn(*a)
         ev1.record(stream)
         torch.cuda.synchronize()
         ms = ev0.elapsed_time(ev1)
@@ -246,36 +270,99 @@ def main():
             ms = float(t.item())
         return n, ms
 
-    # ---- headline: FP32 products, FP64 sums -------------------------------
-    run_steps(warm, hg.FP32)
-    stream.synchronize()
-    clocks = ClockSampler(local_rank)
-    n32, ms32 = timed_run(timed, hg.FP32, res)
-    clk = clocks.stop()
-    res32 = res.clone()
+    # ---- the learned QED weight, trained on this GPU before any timing -----
+    from hlbl_gb300.surrogate import Surrogate
 
-    # ---- plain FP64 on the first fp64-steps timed steps ---------------------
+    sur = Surrogate(device=local_rank, seed=3)
+    t_train = time.perf_counter()
+    train_rep = sur.train(n_samples=args.train_samples, batch=8192, steps=args.train_steps,
+                          n_valid=1 << 18, bound=1e-5)
+    train_rep["wall_seconds"] = round(time.perf_counter() - t_train, 2)
+    train_rep["gain_max_err"] = train_rep["max_rel_err_base"] / max(train_rep["max_rel_err_net"], 1e-300)
+    train_rep["gain_rms_err"] = train_rep["rms_rel_err_base"] / max(train_rep["rms_rel_err_net"], 1e-300)
+
+    # ---- headline: batched, FP32 products, FP64 sums, learned weight, one
+    #      CUDA graph for the timed sources, autotuned tiles and grouping ----
+    c.set_qed(sur)
+    c.reserve(16)
+    y0, xs0, gs0, vs0 = step_args(warm[0] if warm else timed[0])
+    tune = c.autotune(y0, xs0, gs0, vs0, xu, res[:len(xs0)])
+    run_batched(warm, hg.FP32, res)
+    stream.synchronize()
+    c.graph_begin()
+    run_batched(timed, hg.FP32, res)
+    graph = c.graph_end()
+    clocks = ClockSampler(local_rank)
+    n32, ms32 = timeit(lambda: (graph.launch(stream), n_timed_pairs)[1])
+    clk = clocks.stop()
+    res_sur = res.clone()
+    fallbacks = c.qed_fallbacks()
+    graph.close()
+
+    # ---- the same without the graph, and per pair (unbatched) -------------
+    res_b = torch.zeros_like(res)
+    nb_, msb = timeit(run_batched, timed, hg.FP32, res_b)
+    res_p = torch.zeros_like(res)
+    run_pairs(timed[:1], hg.FP32, res_p)
+    npp, mspp = timeit(run_pairs, timed, hg.FP32, res_p)
+
+    # ---- batched FP32 products with the exact FP64 weight -------------------
+    c.set_qed(None)
+    res32x = torch.zeros_like(res)
+    run_batched(timed[:1], hg.FP32, res32x)
+    n32x, ms32x = timeit(run_batched, timed, hg.FP32, res32x)
+
+    # ---- plain FP64, per pair, exact weight (the reference's path) on the
+    #      first fp64-steps steps; the other timed pairs untimed (batched) so
+    #      every timed pair has its FP64 value --------------------------------
     f64_steps = timed[:max(1, args.fp64_steps)]
     res64 = torch.zeros_like(res)
-    run_steps(warm[:1], hg.FP64)
-    n64, ms64 = timed_run(f64_steps, hg.FP64, res64)
-    a32 = res32[:n64].cpu()
-    a64 = res64[:n64].cpu()
-    rel = ((a32 - a64).abs() / a64.abs().clamp_min(1e-300)).max().item()
+    n64, ms64 = timeit(run_pairs, f64_steps, hg.FP64, res64)
+    k = sum(len(s[1]) for s in f64_steps)
+    rest = timed[len(f64_steps):]
+    if rest:
+        run_batched(rest, hg.FP64, res64[k:])
+    stream.synchronize()
+    a64 = res64[:n32].cpu().double()
+
+    def errs(r):
+        """(max per-pair error, the pair's two flavours as one vector;
+        chain-total error of the timed pairs; max per-flavour error)."""
+        a = r[:n32].cpu().double()
+        d = (a - a64).abs()
+        per_pair = (d.max(1).values / a64.abs().max(1).values.clamp_min(1e-300)).max().item()
+        per_flavour = (d / a64.abs().clamp_min(1e-300)).max().item()
+        chain = ((a.sum(0) - a64.sum(0)).abs() / a64.sum(0).abs()).max().item()
+        return per_pair, chain, per_flavour
+
+    rel, chain_rel, rel_fl = errs(res_sur)
+    rel32x, chain32x, rel32x_fl = errs(res32x)
+    relp, _, _ = errs(res_p)
 
     # ---- per-kernel durations (CUDA events on the launching stream) --------
+    c.set_qed(sur)
     c.set_profiling(True)
-    run_steps(timed[:1], hg.FP32)
+    run_batched(timed[:1], hg.FP32, res_b)
     stream.synchronize()
     (p1ms, p1n), (p2ms, p2n) = c.kernel_times()
     c.set_profiling(False)
+    c.set_qed(None)
     c.set_profiling(True)
-    run_steps([(timed[0][0], timed[0][1][:1])], hg.FP64)
+    run_pairs([(timed[0][0], timed[0][1][:1])], hg.FP64, res_b)
     stream.synchronize()
     (p1ms64, p1n64), (p2ms64, p2n64) = c.kernel_times()
     c.set_profiling(False)
+    n_prof = len(timed[0][1])
+    g = tune["batch_group"]
+    groups = [min(g, n_prof - i) for i in range(0, n_prof, g)]
+    # algorithmic bytes of one step's pass-2 launches: y once per launch plus
+    # each partner's block (both flavours, 4,608 B/site per block)
+    step_p2_bytes = sum((1 + gi) for gi in groups) * 2 * 12 * 24 * 8 * volume(LATTICE)
 
-    # ---- end to end through the C ABI with host buffers --------------------
+    # ---- end to end through the C ABI with host buffers: each step stages
+    #      its new block from pinned host memory on the side stream (the
+    #      next one while this one computes) and reads its sums back ---------
+    c.set_qed(sur)
     pinned = {}
     for p, _ in timed:
         site = schedule.mod_pos(p, LATTICE)
@@ -283,19 +370,29 @@ def main():
             h = torch.empty(c.block_length, dtype=torch.float64, pin_memory=True)
             h.copy_(block(p))
             pinned[site] = h
+    host_out = torch.empty((n_timed_pairs, 2), dtype=torch.float64, pin_memory=True)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
     h2d = d2h = 0
-    for p, qs in timed:
-        site = schedule.mod_pos(p, LATTICE)
+    site0 = schedule.mod_pos(timed[0][0], LATTICE)
+    # each source's block has its own device buffer, idle while it is staged
+    c.stage_async(block(timed[0][0]), pinned[site0], pinned[site0].numel() * 8, after_compute=False)
+    h2d += pinned[site0].numel() * 8
+    k = 0
+    for i, st in enumerate(timed):
+        y_b, xs, gs, vs = step_args(st)
+        c.kernel_sums_batched(y_b, xs, gs, vs, xu, res[k:k + len(xs)], hg.FP32)
+        if i + 1 < len(timed):
+            sn = schedule.mod_pos(timed[i + 1][0], LATTICE)
+            c.stage_async(block(timed[i + 1][0]), pinned[sn], pinned[sn].numel() * 8, after_compute=False)
+            h2d += pinned[sn].numel() * 8
         with torch.cuda.stream(stream):
-            block(p).copy_(pinned[site], non_blocking=True)
-        h2d += pinned[site].numel() * 8
-        for q, pp, gx, yv in pairs_of((p, qs)):
-            c.kernel_sum(block(q), block(pp), gx, yv, xu, hg.FP32)  # blocking, result on host
-            d2h += 16
+            host_out[k:k + len(xs)].copy_(res[k:k + len(xs)], non_blocking=True)
+        d2h += len(xs) * 16
+        k += len(xs)
+    stream.synchronize()
     e2e_s = time.perf_counter() - t0
     if dist:
         t = torch.tensor([e2e_s], device="cuda")
@@ -309,9 +406,12 @@ def main():
     V = volume(LATTICE)
     p2_avg_ms = p2ms / max(1, p2n)
     p1_avg_ms = p1ms / max(1, p1n)
-    bytes_launch = BYTES_PER_SITE_PASS * V
-    achieved = bytes_launch / (p2_avg_ms * 1e-3) / 1e9
-    flop_p2 = 2 * V * 2 * (4 * 288 * 160 + 8 * 144 * 3 * 4 + 640)  # both flavours, FMA = 2 flop
+    bytes_launch = step_p2_bytes / max(1, p2n)
+    achieved = step_p2_bytes / (p2ms * 1e-3) / 1e9
+    # pass-2 FLOPs per pair (both flavours, FMA = 2): GEMM 4x288x160, D
+    # formation 8 blocks x 144 x 3 complex MAC, coefficient dot
+    flop_pair = 2 * V * 2 * (4 * 288 * 160 + 8 * 144 * 3 * 4 + 640)
+    flop_p2 = flop_pair * n_prof / max(1, p2n)
     traffic = load_traffic()
 
     pairs_total = n32 * world
@@ -329,20 +429,36 @@ def main():
         "vs_baseline": None,
         "dtype": "fp32 products, fp64 sums",
         "data": "synthetic: seeded i.i.d. complex Gaussian FP64 propagator blocks, generated on the device",
-        "config": {"workload": "24^3x48 (T=48,L=24, V=663552), stride 2, h=(+1,-1,+1,-1), K=4; step = "
-                               "the pairs one new source closes (window 1 sources)",
-                   "lattice": list(LATTICE), "pairs_timed": n32, "path": "per-pair FP32 (batched: not yet)",
-                   "qed_weight": "stand-in (KQED unavailable), exact FP64",
+        "config": {"workload": f"lattice {'x'.join(map(str, LATTICE))} (V={volume(LATTICE)}), stride 2, "
+                               "h=(+1,-1,+1,-1), K=4; step = the pairs one new source closes "
+                               "(window 1 sources)",
+                   "lattice": list(LATTICE), "pairs_timed": n32,
+                   "path": "batched per source (autotuned), one CUDA graph for the timed sources; "
+                           "FP32 products, FP64 sums, learned QED weight",
+                   "qed_weight": "stand-in (KQED unavailable); headline: MLP surrogate with exact "
+                                 "FP64 fallback inside r0",
                    "l2": "inputs 3.06 GB per block, larger than L2; no flush"},
         "fp64": {"value": round(n64 / (ms64 * 1e-3), 4), "unit": "pairs/s", "pairs_timed": n64,
+                 "path": "per pair, FP64 products, exact FP64 weight (the reference's algorithm)",
                  "p2_kernel_ms": round(p2ms64 / max(1, p2n64), 3),
                  "p1_kernel_ms": round(p1ms64 / max(1, p1n64), 3)},
         "speedup_vs_fp64": round(value / (n64 / (ms64 * 1e-3)), 2),
         "max_rel_err_vs_fp64": rel,
+        "max_rel_err_per_flavour_vs_fp64": rel_fl,
+        "chain_total_rel_err_vs_fp64": chain_rel,
+        "batched_fp32_exact_qed": {"value": round(n32x / (ms32x * 1e-3), 4), "unit": "pairs/s",
+                                   "max_rel_err_vs_fp64": rel32x, "chain_total_rel_err_vs_fp64": chain32x,
+                                   "max_rel_err_per_flavour_vs_fp64": rel32x_fl},
+        "batched_surrogate_no_graph": {"value": round(nb_ / (msb * 1e-3), 4), "unit": "pairs/s"},
+        "per_pair_fp32_surrogate": {"value": round(npp / (mspp * 1e-3), 4), "unit": "pairs/s",
+                                    "max_rel_err_vs_fp64": relp},
+        "autotune": tune,
+        "surrogate": {"train": train_rep, "fallback_rows_timed": fallbacks,
+                      "rows_timed": n32 * 3 * volume(LATTICE)},
         "e2e": {"value": round(pairs_total / e2e_s, 4), "unit": "pairs/s",
                 "h2d_bytes_per_step": int(h2d / max(1, len(timed))),
                 "d2h_bytes_per_step": int(d2h / max(1, len(timed)))},
-        "roofline": {"bound": "hbm", "kernel": "p2_kernel<float,2,8>",
+        "roofline": {"bound": "hbm", "kernel": f"p2_kernel<float,2,{4 if tune['p2_tile'] == 4 else 8}> (batched)",
                      "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / peaks["hbm_gbs"], 5),
                      "traffic": (traffic or {}).get("bytes_per_launch"),
@@ -356,7 +472,7 @@ def main():
                              "fp64_p2_tflops": round(flop_p2 / (p2ms64 / max(1, p2n64) * 1e-3) / 1e12, 4),
                              "peak_source": "measured here (FMA-chain kernel, hlbl_measure_fma_peak)"},
         "clocks": clk,
-        "gpu_launches": n32 * 6,
+        "gpu_launches": sum(7 * len([0 for _ in range(0, len(s[1]), tune["batch_group"])]) for s in timed),
     }
 
     if rank == 0 and not args.no_cpu_baseline:

@@ -13,6 +13,21 @@ from .build import LIB
 I4 = C.c_int * 4
 
 
+class TrainConfig(C.Structure):
+    """hlbl_train_config (include/hlbl_gb300.h)."""
+    _fields_ = [("n_samples", C.c_longlong), ("batch", C.c_int), ("steps", C.c_int),
+                ("lr", C.c_float), ("seed", C.c_uint64), ("radius", C.c_float),
+                ("n_valid", C.c_longlong), ("bound", C.c_double)]
+
+
+class TrainReport(C.Structure):
+    """hlbl_train_report (include/hlbl_gb300.h)."""
+    _fields_ = [("final_loss", C.c_float), ("max_rel_err_net", C.c_double),
+                ("rms_rel_err_net", C.c_double), ("max_rel_err_base", C.c_double),
+                ("rms_rel_err_base", C.c_double), ("r0", C.c_double),
+                ("train_seconds", C.c_double), ("r1", C.c_double)]
+
+
 class HlblError(RuntimeError):
     """A C-ABI call returned a nonzero status."""
 
@@ -32,6 +47,8 @@ def _load() -> C.CDLL:
         "hlbl_ctx_create": (C.c_int, [C.POINTER(vp), i4p, i4p, i4p, C.c_double, C.c_int]),
         "hlbl_ctx_destroy": (None, [vp]),
         "hlbl_ctx_set_stream": (C.c_int, [vp, vp]),
+        "hlbl_ctx_check": (C.c_int, [vp]),
+        "hlbl_selftest_wait_timeout": (C.c_int, [vp]),
         "hlbl_kernel_sum": (C.c_int, [vp, vp, vp, i4p, i4p, C.c_double, C.c_int, dp]),
         "hlbl_kernel_sum_async": (C.c_int, [vp, vp, vp, i4p, i4p, C.c_double, C.c_int, vp]),
         "hlbl_cu_dzu_dzsu": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, i4p, i4p, i4p, i4p]),
@@ -45,6 +62,25 @@ def _load() -> C.CDLL:
         "hlbl_source_seed": (C.c_uint64, [C.c_uint64, i4p]),
         "hlbl_block_length": (C.c_size_t, [vp]),
         "hlbl_ctx_set_profiling": (C.c_int, [vp, C.c_int]),
+        "hlbl_kernel_sums_batched": (C.c_int, [vp, vp, C.c_int, C.POINTER(vp), i4p, i4p,
+                                               C.c_double, C.c_int, vp]),
+        "hlbl_ctx_set_batch_group": (C.c_int, [vp, C.c_int]),
+        "hlbl_ctx_reserve": (C.c_int, [vp, C.c_int]),
+        "hlbl_stage_async": (C.c_int, [vp, vp, vp, C.c_size_t, C.c_int]),
+        "hlbl_autotune": (C.c_int, [vp, vp, C.c_int, C.POINTER(vp), i4p, i4p, C.c_double, vp,
+                                    C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), dp]),
+        "hlbl_graph_begin": (C.c_int, [vp]),
+        "hlbl_graph_end": (C.c_int, [vp, C.POINTER(vp)]),
+        "hlbl_graph_launch": (C.c_int, [vp, vp]),
+        "hlbl_graph_destroy": (None, [vp]),
+        "hlbl_surrogate_create": (C.c_int, [C.POINTER(vp), C.c_int, C.c_double, C.c_uint64]),
+        "hlbl_surrogate_destroy": (None, [vp]),
+        "hlbl_surrogate_train": (C.c_int, [vp, C.POINTER(TrainConfig), C.POINTER(TrainReport)]),
+        "hlbl_surrogate_params": (C.c_int, [vp, vp, vp, C.c_int]),
+        "hlbl_surrogate_gradients": (C.c_int, [vp, vp, vp, C.c_int, vp, C.POINTER(C.c_float)]),
+        "hlbl_surrogate_eval": (C.c_int, [vp, vp, C.c_int, vp]),
+        "hlbl_ctx_set_qed": (C.c_int, [vp, C.c_int, vp, C.c_double]),
+        "hlbl_ctx_qed_fallbacks": (C.c_int, [vp, C.POINTER(C.c_ulonglong)]),
         "hlbl_ctx_kernel_times": (C.c_int, [vp, dp, C.POINTER(C.c_longlong)]),
         "hlbl_measure_fma_peak": (C.c_int, [C.c_int, C.c_int, dp]),
     }

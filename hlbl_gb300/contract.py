@@ -40,6 +40,25 @@ def _prec(p) -> int:
     raise ValueError(f"precision must be fp64 or fp32, not {p!r}")
 
 
+class Graph:
+    """A recorded window (hlbl_graph): replay with launch()."""
+
+    def __init__(self, h):
+        self._h = h
+
+    def launch(self, stream=None) -> None:
+        raw = getattr(stream, "cuda_stream", stream)
+        check(lib.hlbl_graph_launch(self._h, C.c_void_p(raw) if raw else None))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib.hlbl_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
 class Contractor:
     """Kernel sums of pairs of point sources (src/contract.cpp of the reference)."""
 
@@ -87,6 +106,10 @@ class Contractor:
         """Doubles in one propagator block (provider.hpp:18-20)."""
         return int(lib.hlbl_block_length(self._h))
 
+    def check(self) -> None:
+        """Raise if a kernel gave up a bounded wait since the last check."""
+        check(lib.hlbl_ctx_check(self._h))
+
     def set_stream(self, stream) -> None:
         """Run on a CUDA stream (torch.cuda.Stream, a raw handle, or None)."""
         raw = getattr(stream, "cuda_stream", stream)
@@ -108,6 +131,52 @@ class Contractor:
         """As kernel_sum, results written to the device buffer d_out[2]."""
         check(lib.hlbl_kernel_sum_async(self._h, ptr(d_fwd_src), ptr(d_fwd_y), i4(gsx), i4(yv),
                                         C.c_double(xunit), _prec(precision), ptr(d_out)))
+
+    def kernel_sums_batched(self, d_fwd_y, d_srcs, gsxs, yvs, xunit: float, d_out,
+                            precision=FP64) -> None:
+        """All pairs one new source closes: pair i = (gsxs[i], gsxs[i] + yvs[i])
+        with partner block d_srcs[i]; sums to the device buffer d_out[n][2].
+        Asynchronous on the context's stream (batched launches share y)."""
+        n = len(d_srcs)
+        srcs = (C.c_void_p * max(1, n))(*[ptr(s) for s in d_srcs])
+        g = (C.c_int * (4 * max(1, n)))(*[int(v) for p in gsxs for v in p])
+        y = (C.c_int * (4 * max(1, n)))(*[int(v) for p in yvs for v in p])
+        check(lib.hlbl_kernel_sums_batched(self._h, ptr(d_fwd_y), n, srcs, g, y, C.c_double(xunit),
+                                           _prec(precision), ptr(d_out)))
+
+    def reserve(self, max_pairs: int) -> None:
+        check(lib.hlbl_ctx_reserve(self._h, int(max_pairs)))
+
+    def stage_async(self, d_dst, h_src, nbytes: int, after_compute: bool = True) -> None:
+        """Copy a pinned host block to the device on the side stream; the next
+        contraction waits for it (host-cache staging). after_compute: wait
+        first for contraction work already enqueued (d_dst may be in use)."""
+        check(lib.hlbl_stage_async(self._h, ptr(d_dst), ptr(h_src), int(nbytes),
+                                   1 if after_compute else 0))
+
+    def autotune(self, d_fwd_y, d_srcs, gsxs, yvs, xunit: float, d_out) -> dict:
+        """Pick the FP32 tile variants and batch group on this batch."""
+        n = len(d_srcs)
+        srcs = (C.c_void_p * n)(*[ptr(s) for s in d_srcs])
+        g = (C.c_int * (4 * n))(*[int(v) for p in gsxs for v in p])
+        y = (C.c_int * (4 * n))(*[int(v) for p in yvs for v in p])
+        p1, p2, grp, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        check(lib.hlbl_autotune(self._h, ptr(d_fwd_y), n, srcs, g, y, C.c_double(xunit), ptr(d_out),
+                                C.byref(p1), C.byref(p2), C.byref(grp), C.byref(ms)))
+        return {"p1_tile": 16 if p1.value else 32, "p2_tile": 4 if p2.value else 8,
+                "batch_group": grp.value, "ms": ms.value}
+
+    def graph_begin(self) -> None:
+        check(lib.hlbl_graph_begin(self._h))
+
+    def graph_end(self) -> "Graph":
+        g = C.c_void_p()
+        check(lib.hlbl_graph_end(self._h, C.byref(g)))
+        return Graph(g)
+
+    def set_batch_group(self, group: int) -> None:
+        """Pairs per batched launch (1..16; 0 = 16)."""
+        check(lib.hlbl_ctx_set_batch_group(self._h, int(group)))
 
     # -- the vendored launchers (kernels/cuda_lattice.h:49-57) -------------
     def cu_dzu_dzsu(self, d_dzu, d_dzsu, fwd_src, fwd_y, iflavor, proc_coords, gsx,
@@ -138,6 +207,20 @@ class Contractor:
         """Contractor::pieces_2p2 (contract.cpp:116-156) is not part of this
         library: the 2+2 pieces are a different contraction."""
         raise NotImplementedError("the 2+2 pieces (compute_2p2_gpu) are not implemented here")
+
+    # -- the QED weight ------------------------------------------------------
+    def set_qed(self, surrogate=None, r0: float = -1.0) -> None:
+        """Pass 2's QED weight: the exact stand-in (surrogate None) or the
+        learned surrogate with fallback radius r0 (< 0: its validated radius)."""
+        if surrogate is None:
+            check(lib.hlbl_ctx_set_qed(self._h, 0, None, C.c_double(0.0)))
+        else:
+            check(lib.hlbl_ctx_set_qed(self._h, 1, surrogate.handle, C.c_double(r0)))
+
+    def qed_fallbacks(self) -> int:
+        n = C.c_ulonglong()
+        check(lib.hlbl_ctx_qed_fallbacks(self._h, C.byref(n)))
+        return int(n.value)
 
     # -- measurement ---------------------------------------------------------
     def set_profiling(self, on: bool) -> None:

@@ -21,6 +21,16 @@ thread_local std::string g_last_error;
 }  // namespace
 
 namespace hg {
+namespace sur {
+// surrogate.cu: pass 2's weights from the learned surrogate
+int launch_surrogate_weights(const hlbl_surrogate* s, const Geometry& geo, const WArgs& wa,
+                             double r0, double* d_w, unsigned long long* d_fallback,
+                             cudaStream_t st, int nsm);
+double surrogate_r0(const hlbl_surrogate* s);
+}  // namespace sur
+}  // namespace hg
+
+namespace hg {
 
 int fail(int code, const char* fmt, ...) {
   char buf[512];
@@ -77,6 +87,21 @@ __global__ void fill_gaussian_kernel(double* __restrict__ out, Geometry geo, uin
   }
 }
 
+// Diagnostic for the bounded waits: an mbarrier told to expect 16 bytes that
+// never come, so the phase never completes; the wait gives up, sets the
+// error flag and the kernel returns (nothing is in flight).
+__global__ void wait_timeout_selftest_kernel(int* err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    mbar_arrive_expect_tx(&bar, 16);
+  }
+  __syncthreads();
+  bool const ok = mbar_wait(&bar, 0);
+  if (!ok && threadIdx.x == 0) atomicExch(err, kErrWaitTimeout);
+}
+
 // ---- launch plumbing -------------------------------------------------------
 template <typename T, int NF, int TS>
 struct P1Launch {
@@ -93,9 +118,9 @@ struct P1Launch {
     grid = nb * nsm;
     return HLBL_OK;
   }
-  static void launch(int grid, cudaStream_t st, const double* src, const double* y,
-                     const Geometry& geo, int4 gsx, int f0, double* partials) {
-    p1_kernel<T, NF, TS><<<grid, threads, smem, st>>>(src, y, geo, gsx, f0, partials);
+  static void launch(int grid, cudaStream_t st, const double* y, const PairBatch& b,
+                     const Geometry& geo, int f0, double* partials, int* err) {
+    p1_kernel<T, NF, TS><<<dim3(grid, b.n), threads, smem, st>>>(y, b, geo, f0, partials, err);
   }
   static long long tiles(long long V) { return (V + TS - 1) / TS; }
 };
@@ -115,22 +140,25 @@ struct P2Launch {
     grid = nb * nsm;
     return HLBL_OK;
   }
-  static void launch(int grid, cudaStream_t st, const double* src, const double* y,
-                     const Geometry& geo, const P2Args& a, const T* bt, double* partials) {
-    p2_kernel<T, NF, TS><<<grid, threads, smem, st>>>(src, y, geo, a, bt, partials);
+  static void launch(int grid, cudaStream_t st, const double* y, const PairBatch& b,
+                     const Geometry& geo, const P2Args& a, const T* bt, double* partials, int* err) {
+    p2_kernel<T, NF, TS><<<dim3(grid, b.n), threads, smem, st>>>(y, b, geo, a, bt, partials, err);
   }
   static long long tiles(long long V) { return (V + TS - 1) / TS; }
 };
 
-// tile sizes per precision
-using P1D2 = P1Launch<double, 2, 16>;
-using P1D1 = P1Launch<double, 1, 16>;
-using P1F2 = P1Launch<float, 2, 32>;
-using P1F1 = P1Launch<float, 1, 32>;
+// tile sizes per precision (the FP32 two-flavour kernels have a second tile
+// size each, which the autotuner may choose)
+using P1D2 = P1Launch<double, 2, 8>;
+using P1D1 = P1Launch<double, 1, 8>;
+using P1F2 = P1Launch<float, 2, 8>;
+using P1F2s = P1Launch<float, 2, 4>;
+using P1F1 = P1Launch<float, 1, 8>;
 using P2D2 = P2Launch<double, 2, 4>;
 using P2D1 = P2Launch<double, 1, 4>;
-using P2F2 = P2Launch<float, 2, 8>;
-using P2F1 = P2Launch<float, 1, 8>;
+using P2F2 = P2Launch<float, 2, 4>;
+using P2F2s = P2Launch<float, 2, 2>;
+using P2F1 = P2Launch<float, 1, 4>;
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
@@ -162,16 +190,31 @@ struct hlbl_ctx {
   cudaStream_t stream = nullptr;
   Geometry geo{};
   hlbl_qed_params qp{};
-  int grid_p1d2 = 0, grid_p1d1 = 0, grid_p1f2 = 0, grid_p1f1 = 0;
-  int grid_p2d2 = 0, grid_p2d1 = 0, grid_p2f2 = 0, grid_p2f1 = 0;
+  int grid_p1d2 = 0, grid_p1d1 = 0, grid_p1f2 = 0, grid_p1f1 = 0, grid_p1f2s = 0;
+  int grid_p2d2 = 0, grid_p2d1 = 0, grid_p2f2 = 0, grid_p2f1 = 0, grid_p2f2s = 0;
+  int p1_small = 0, p2_small = 0;  // FP32 tile variants chosen (autotuner)
+  // staging of host blocks on a side stream (hlbl_stage_async)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t stage_ev = nullptr;
+  cudaEvent_t compute_ev = nullptr;
+  bool stage_pending = false;
+  bool capturing = false;
   int max_grid = 0;
   double* d_part1 = nullptr;  // [max_grid][2][2880]
   double* d_part2 = nullptr;  // [max_grid][2]
   double* d_dz = nullptr;     // [2][2880]
   double* d_g = nullptr;      // [2][11520]
   void* d_bt = nullptr;       // [2][288*160] of double (float uses half of it)
+  double* d_w = nullptr;      // QED weights [V][3][6]
+  long long w_cap = 0;        // sites d_w holds
+  int batch_group = 0;        // pairs per batched launch (0: kMaxBatch)
+  int qed_mode = HLBL_QED_EXACT;
+  const hlbl_surrogate* sur = nullptr;
+  double sur_r0 = 0.0;
+  unsigned long long* d_fallback = nullptr;  // rows evaluated exactly inside r0
   double* d_out = nullptr;    // [2]
   double* h_out = nullptr;    // pinned [2]
+  int* d_err = nullptr;       // kernels' error flag (a bounded wait gave up)
   // optional per-kernel timing with CUDA events on the launching stream
   bool profiling = false;
   cudaEvent_t ev[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [pass][begin/end]
@@ -195,69 +238,119 @@ void prof_collect(hlbl_ctx* c, int pass) {
   c->prof_pending[pass] = 0;
 }
 void prof_begin(hlbl_ctx* c, int pass) {
-  if (!c->profiling) return;
+  if (!c->profiling || c->capturing) return;
   prof_collect(c, pass);
   cudaEventRecord(c->ev[pass][0], c->stream);
 }
 void prof_end(hlbl_ctx* c, int pass) {
-  if (!c->profiling) return;
+  if (!c->profiling || c->capturing) return;
   cudaEventRecord(c->ev[pass][1], c->stream);
   c->prof_pending[pass] = 1;
 }
 
-// Pass 1 + reduction + gamma insertion + Bt for flavours [f0, f0+nf).
-// g_dzu/g_dzsu of flavour fl land at d_g + fl*kGLen (+kGDzuLen).
-int run_pass1(hlbl_ctx* c, const Geometry& geo, const double* src, const double* y,
-              const int gsx[4], int f0, int nf, int precision, double* add_dzu,
-              double* add_dzsu, bool build_bt) {
-  int4 const g4 = make_int4(gsx[0], gsx[1], gsx[2], gsx[3]);
+// Thread blocks per pair: the resident grid shared among the batch's pairs,
+// at most one tile each.
+int per_pair_grid(int resident, int npairs, long long tiles) {
+  long long g = std::max(1, resident / std::max(1, npairs));
+  return (int)std::min(g, tiles);
+}
+
+// Pass 1 + reduction + gamma insertion + Bt for the batch's pairs, flavours
+// [f0, f0+nf). Pair i, flavour fl: dz at d_dz + (i*nf + fl)*kDzLen, g at
+// d_g + (i*nf + fl)*kGLen, Bt at d_bt + (i*nf + fl)*kBtK*kBtN.
+int run_pass1(hlbl_ctx* c, const Geometry& geo, const double* y, const PairBatch& b, int f0,
+              int nf, int precision, double* add_dzu, double* add_dzsu, bool build_bt) {
+  if (c->stage_pending) {  // blocks staged on the side stream must have landed
+    cudaError_t e = cudaStreamWaitEvent(c->stream, c->stage_ev, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "wait for staged block");
+    c->stage_pending = false;
+  }
   int grid;
   prof_begin(c, 0);
   if (precision == HLBL_FP64) {
-    if (nf == 2) { grid = (int)std::min<long long>(c->grid_p1d2, P1D2::tiles(geo.V)); P1D2::launch(grid, c->stream, src, y, geo, g4, f0, c->d_part1); }
-    else { grid = (int)std::min<long long>(c->grid_p1d1, P1D1::tiles(geo.V)); P1D1::launch(grid, c->stream, src, y, geo, g4, f0, c->d_part1); }
+    if (nf == 2) { grid = per_pair_grid(c->grid_p1d2, b.n, P1D2::tiles(geo.V)); P1D2::launch(grid, c->stream, y, b, geo, f0, c->d_part1, c->d_err); }
+    else { grid = per_pair_grid(c->grid_p1d1, b.n, P1D1::tiles(geo.V)); P1D1::launch(grid, c->stream, y, b, geo, f0, c->d_part1, c->d_err); }
   } else {
-    if (nf == 2) { grid = (int)std::min<long long>(c->grid_p1f2, P1F2::tiles(geo.V)); P1F2::launch(grid, c->stream, src, y, geo, g4, f0, c->d_part1); }
-    else { grid = (int)std::min<long long>(c->grid_p1f1, P1F1::tiles(geo.V)); P1F1::launch(grid, c->stream, src, y, geo, g4, f0, c->d_part1); }
+    if (nf == 2 && c->p1_small) { grid = per_pair_grid(c->grid_p1f2s, b.n, P1F2s::tiles(geo.V)); P1F2s::launch(grid, c->stream, y, b, geo, f0, c->d_part1, c->d_err); }
+    else if (nf == 2) { grid = per_pair_grid(c->grid_p1f2, b.n, P1F2::tiles(geo.V)); P1F2::launch(grid, c->stream, y, b, geo, f0, c->d_part1, c->d_err); }
+    else { grid = per_pair_grid(c->grid_p1f1, b.n, P1F1::tiles(geo.V)); P1F1::launch(grid, c->stream, y, b, geo, f0, c->d_part1, c->d_err); }
   }
   prof_end(c, 0);
-  p1_reduce_kernel<<<dim3((kDzLen + 255) / 256, nf), 256, 0, c->stream>>>(c->d_part1, grid, nf, c->d_dz,
-                                                                          add_dzu, add_dzsu);
+  p1_reduce_kernel<<<dim3((kDzLen + 255) / 256, nf, b.n), 256, 0, c->stream>>>(
+      c->d_part1, grid, nf, c->d_dz, add_dzu, add_dzsu);
   if (!build_bt) return HLBL_OK;
-  g_build_kernel<<<dim3((kGLen / 2 + 255) / 256, nf), 256, 0, c->stream>>>(c->d_dz, nf, c->d_g);
+  g_build_kernel<<<dim3((kGLen / 2 + 255) / 256, nf, b.n), 256, 0, c->stream>>>(c->d_dz, nf, c->d_g);
+  dim3 const gb((kBtK * kBtN + 255) / 256, nf, b.n);
   if (precision == HLBL_FP64)
-    bt_build_kernel<double><<<dim3((kBtK * kBtN + 255) / 256, nf), 256, 0, c->stream>>>(
-        c->d_g, c->d_g + kGDzuLen, kGLen, nf, static_cast<double*>(c->d_bt));
+    bt_build_kernel<double><<<gb, 256, 0, c->stream>>>(c->d_g, c->d_g + kGDzuLen, kGLen,
+                                                       (size_t)nf * kGLen, nf, static_cast<double*>(c->d_bt));
   else
-    bt_build_kernel<float><<<dim3((kBtK * kBtN + 255) / 256, nf), 256, 0, c->stream>>>(
-        c->d_g, c->d_g + kGDzuLen, kGLen, nf, static_cast<float*>(c->d_bt));
+    bt_build_kernel<float><<<gb, 256, 0, c->stream>>>(c->d_g, c->d_g + kGDzuLen, kGLen,
+                                                      (size_t)nf * kGLen, nf, static_cast<float*>(c->d_bt));
   return HLBL_OK;
 }
 
-// Pass 2 for flavours [f0, f0+nf) with Bt already built; reduces into
-// out[0..nf) (added if add).
-int run_pass2(hlbl_ctx* c, const Geometry& geo, const double* src, const double* y,
-              const int gsx[4], const int yv[4], double xunit, int f0, int nf, int precision,
-              double* out, int add) {
+// The QED weights of the batch's pairs into d_w ([pair][V][3][6]).
+int run_weights(hlbl_ctx* c, const Geometry& geo, const PairBatch& b, double xunit) {
+  long long const need = geo.V * b.n;
+  if (need > c->w_cap) {
+    if (c->capturing) return fail(HLBL_ESTATE, "QED weight buffer too small during graph capture");
+    cudaFree(c->d_w);
+    c->d_w = nullptr;
+    c->w_cap = 0;
+    cudaError_t e = cudaMalloc(&c->d_w, sizeof(double) * 3 * HLBL_QED_NW * (size_t)need);
+    if (e != cudaSuccess) return fail(HLBL_ENOMEM, "QED weight buffer: %s", cudaGetErrorString(e));
+    c->w_cap = need;
+  }
+  WArgs wa{};
+  wa.batch = b;
+  wa.xunit = xunit;
+  wa.qp = c->qp;
+  if (c->qed_mode == HLBL_QED_SURROGATE)
+    return sur::launch_surrogate_weights(c->sur, geo, wa, c->sur_r0, c->d_w, c->d_fallback, c->stream,
+                                         c->nsm);
+  long long const n = geo.V * 3;
+  int const blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)c->nsm * 16 / b.n));
+  qed_weights_exact_kernel<<<dim3(blocks, b.n), 256, 0, c->stream>>>(geo, wa, c->d_w);
+  return HLBL_OK;
+}
+
+// Pass 2 for the batch's pairs with Bt already built; pair i's sums go to
+// b.p[i].out[0..nf) (added if add).
+int run_pass2(hlbl_ctx* c, const Geometry& geo, const double* y, const PairBatch& b, double xunit,
+              int f0, int nf, int precision, int add) {
+  if (int rc = run_weights(c, geo, b, xunit)) return rc;
   P2Args a{};
-  for (int r = 0; r < 4; ++r) { a.gsx[r] = gsx[r]; a.yv[r] = yv[r]; }
   a.xunit = xunit;
   a.f0 = f0;
-  a.qp = c->qp;
+  a.w = c->d_w;
   int grid;
   prof_begin(c, 1);
   if (precision == HLBL_FP64) {
     const double* bt = static_cast<const double*>(c->d_bt);
-    if (nf == 2) { grid = (int)std::min<long long>(c->grid_p2d2, P2D2::tiles(geo.V)); P2D2::launch(grid, c->stream, src, y, geo, a, bt, c->d_part2); }
-    else { grid = (int)std::min<long long>(c->grid_p2d1, P2D1::tiles(geo.V)); P2D1::launch(grid, c->stream, src, y, geo, a, bt, c->d_part2); }
+    if (nf == 2) { grid = per_pair_grid(c->grid_p2d2, b.n, P2D2::tiles(geo.V)); P2D2::launch(grid, c->stream, y, b, geo, a, bt, c->d_part2, c->d_err); }
+    else { grid = per_pair_grid(c->grid_p2d1, b.n, P2D1::tiles(geo.V)); P2D1::launch(grid, c->stream, y, b, geo, a, bt, c->d_part2, c->d_err); }
   } else {
     const float* bt = static_cast<const float*>(c->d_bt);
-    if (nf == 2) { grid = (int)std::min<long long>(c->grid_p2f2, P2F2::tiles(geo.V)); P2F2::launch(grid, c->stream, src, y, geo, a, bt, c->d_part2); }
-    else { grid = (int)std::min<long long>(c->grid_p2f1, P2F1::tiles(geo.V)); P2F1::launch(grid, c->stream, src, y, geo, a, bt, c->d_part2); }
+    if (nf == 2 && c->p2_small) { grid = per_pair_grid(c->grid_p2f2s, b.n, P2F2s::tiles(geo.V)); P2F2s::launch(grid, c->stream, y, b, geo, a, bt, c->d_part2, c->d_err); }
+    else if (nf == 2) { grid = per_pair_grid(c->grid_p2f2, b.n, P2F2::tiles(geo.V)); P2F2::launch(grid, c->stream, y, b, geo, a, bt, c->d_part2, c->d_err); }
+    else { grid = per_pair_grid(c->grid_p2f1, b.n, P2F1::tiles(geo.V)); P2F1::launch(grid, c->stream, y, b, geo, a, bt, c->d_part2, c->d_err); }
   }
   prof_end(c, 1);
-  p2_reduce_kernel<<<1, 32, 0, c->stream>>>(c->d_part2, grid, nf, out, add);
+  p2_reduce_kernel<<<b.n, 32, 0, c->stream>>>(c->d_part2, grid, nf, b, add);
   return HLBL_OK;
+}
+
+PairBatch one_pair(const double* src, double* out, const int gsx[4], const int yv[4]) {
+  PairBatch b{};
+  b.n = 1;
+  b.p[0].src = src;
+  b.p[0].out = out;
+  for (int r = 0; r < 4; ++r) {
+    b.p[0].gsx[r] = gsx[r];
+    b.p[0].yv[r] = yv ? yv[r] : 0;
+  }
+  return b;
 }
 
 int check_launch(const char* what) {
@@ -297,24 +390,35 @@ int hlbl_ctx_create(hlbl_ctx** out, const int global[4], const int local[4],
   if ((rc = P1D2::init(c->nsm, c->grid_p1d2)) || (rc = P1D1::init(c->nsm, c->grid_p1d1)) ||
       (rc = P1F2::init(c->nsm, c->grid_p1f2)) || (rc = P1F1::init(c->nsm, c->grid_p1f1)) ||
       (rc = P2D2::init(c->nsm, c->grid_p2d2)) || (rc = P2D1::init(c->nsm, c->grid_p2d1)) ||
-      (rc = P2F2::init(c->nsm, c->grid_p2f2)) || (rc = P2F1::init(c->nsm, c->grid_p2f1)))
+      (rc = P2F2::init(c->nsm, c->grid_p2f2)) || (rc = P2F1::init(c->nsm, c->grid_p2f1)) ||
+      (rc = P1F2s::init(c->nsm, c->grid_p1f2s)) || (rc = P2F2s::init(c->nsm, c->grid_p2f2s)))
     return bail(rc);
   c->max_grid = std::max({c->grid_p1d2, c->grid_p1d1, c->grid_p1f2, c->grid_p1f1, c->grid_p2d2,
-                          c->grid_p2d1, c->grid_p2f2, c->grid_p2f1});
+                          c->grid_p2d1, c->grid_p2f2, c->grid_p2f1, c->grid_p1f2s, c->grid_p2f2s});
+  e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->stage_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->compute_ev, cudaEventDisableTiming);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "copy stream"));
   e = cudaStreamCreate(&c->own_stream);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
   c->stream = c->own_stream;
+  // per-pair work buffers for up to kMaxBatch pairs; the partial sums of a
+  // batch never exceed max(resident grid, kMaxBatch) thread blocks
+  size_t const slots = (size_t)std::max(c->max_grid, kMaxBatch);
   struct { void** p; size_t n; } bufs[] = {
-      {(void**)&c->d_part1, sizeof(double) * (size_t)c->max_grid * 2 * kDzLen},
-      {(void**)&c->d_part2, sizeof(double) * (size_t)c->max_grid * 2},
-      {(void**)&c->d_dz, sizeof(double) * 2 * kDzLen},
-      {(void**)&c->d_g, sizeof(double) * 2 * kGLen},
-      {(void**)&c->d_bt, sizeof(double) * 2 * kBtK * kBtN},
-      {(void**)&c->d_out, sizeof(double) * 2}};
+      {(void**)&c->d_part1, sizeof(double) * slots * 2 * kDzLen},
+      {(void**)&c->d_part2, sizeof(double) * slots * 2},
+      {(void**)&c->d_dz, sizeof(double) * kMaxBatch * 2 * kDzLen},
+      {(void**)&c->d_g, sizeof(double) * kMaxBatch * 2 * kGLen},
+      {(void**)&c->d_bt, sizeof(double) * kMaxBatch * 2 * kBtK * kBtN},
+      {(void**)&c->d_out, sizeof(double) * 2},
+      {(void**)&c->d_err, sizeof(int)}};
   for (auto& b : bufs) {
     e = cudaMalloc(b.p, b.n);
     if (e != cudaSuccess) return bail(fail(HLBL_ENOMEM, "cudaMalloc %zu bytes: %s", b.n, cudaGetErrorString(e)));
   }
+  e = cudaMemset(c->d_err, 0, sizeof(int));
+  if (e != cudaSuccess) return bail(cuda_fail(e, "error flag"));
   e = cudaMallocHost(reinterpret_cast<void**>(&c->h_out), sizeof(double) * 2);
   if (e != cudaSuccess) return bail(fail(HLBL_ENOMEM, "cudaMallocHost: %s", cudaGetErrorString(e)));
   *out = c;
@@ -331,12 +435,38 @@ void hlbl_ctx_destroy(hlbl_ctx* c) {
   cudaFree(c->d_g);
   cudaFree(c->d_bt);
   cudaFree(c->d_out);
+  cudaFree(c->d_err);
+  cudaFree(c->d_w);
+  cudaFree(c->d_fallback);
   if (c->h_out) cudaFreeHost(c->h_out);
   for (auto& pe : c->ev)
     for (auto& e : pe)
       if (e) cudaEventDestroy(e);
+  if (c->copy_stream) { cudaStreamSynchronize(c->copy_stream); cudaStreamDestroy(c->copy_stream); }
+  if (c->stage_ev) cudaEventDestroy(c->stage_ev);
+  if (c->compute_ev) cudaEventDestroy(c->compute_ev);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
+}
+
+int hlbl_selftest_wait_timeout(hlbl_ctx* c) {
+  if (!c) return fail(HLBL_EINVAL, "hlbl_selftest_wait_timeout: null context");
+  wait_timeout_selftest_kernel<<<1, 32, 0, c->stream>>>(c->d_err);
+  return check_launch("hlbl_selftest_wait_timeout launch");
+}
+
+int hlbl_ctx_check(hlbl_ctx* c) {
+  if (!c) return fail(HLBL_EINVAL, "hlbl_ctx_check: null context");
+  int flag = 0;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(&flag, c->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "hlbl_ctx_check");
+  if (flag) {
+    cudaMemset(c->d_err, 0, sizeof(int));
+    return fail(HLBL_ECUDA, "a contraction kernel gave up waiting for its staged tile (code %d); "
+                            "the sums since the last check are invalid", flag);
+  }
+  return HLBL_OK;
 }
 
 int hlbl_ctx_set_stream(hlbl_ctx* c, void* stream) {
@@ -354,9 +484,49 @@ int hlbl_kernel_sum_async(hlbl_ctx* c, const double* src, const double* y, const
   if (precision != HLBL_FP64 && precision != HLBL_FP32) return fail(HLBL_EINVAL, "hlbl_kernel_sum: bad precision %d", precision);
   for (int r = 0; r < 4; ++r)
     if (gsx[r] < 0 || gsx[r] >= c->geo.global[r]) return fail(HLBL_EINVAL, "hlbl_kernel_sum: gsx[%d] = %d outside [0, %d)", r, gsx[r], c->geo.global[r]);
-  if (int rc = run_pass1(c, c->geo, src, y, gsx, 0, 2, precision, nullptr, nullptr, true)) return rc;
-  if (int rc = run_pass2(c, c->geo, src, y, gsx, yv, xunit, 0, 2, precision, d_out, 0)) return rc;
+  PairBatch const b = one_pair(src, d_out, gsx, yv);
+  if (int rc = run_pass1(c, c->geo, y, b, 0, 2, precision, nullptr, nullptr, true)) return rc;
+  if (int rc = run_pass2(c, c->geo, y, b, xunit, 0, 2, precision, 0)) return rc;
   return check_launch("hlbl_kernel_sum launch");
+}
+
+int hlbl_kernel_sums_batched(hlbl_ctx* c, const double* y, int n, const double* const* srcs,
+                             const int* gsx, const int* yv, double xunit, int precision,
+                             double* d_out) {
+  if (!c || !y || !srcs || !gsx || !yv || !d_out || n < 0)
+    return fail(HLBL_EINVAL, "hlbl_kernel_sums_batched: bad argument");
+  if (precision != HLBL_FP64 && precision != HLBL_FP32)
+    return fail(HLBL_EINVAL, "hlbl_kernel_sums_batched: bad precision %d", precision);
+  if (!aligned16(y)) return fail(HLBL_EINVAL, "hlbl_kernel_sums_batched: blocks must be 16-byte aligned");
+  for (int i = 0; i < n; ++i) {
+    if (!srcs[i] || !aligned16(srcs[i]))
+      return fail(HLBL_EINVAL, "hlbl_kernel_sums_batched: block %d null or not 16-byte aligned", i);
+    for (int r = 0; r < 4; ++r)
+      if (gsx[4 * i + r] < 0 || gsx[4 * i + r] >= c->geo.global[r])
+        return fail(HLBL_EINVAL, "hlbl_kernel_sums_batched: gsx of pair %d outside the lattice", i);
+  }
+  int const group = c->batch_group > 0 ? std::min(c->batch_group, kMaxBatch) : kMaxBatch;
+  for (int i0 = 0; i0 < n; i0 += group) {
+    PairBatch b{};
+    b.n = std::min(group, n - i0);
+    for (int i = 0; i < b.n; ++i) {
+      b.p[i].src = srcs[i0 + i];
+      b.p[i].out = d_out + 2 * (size_t)(i0 + i);
+      for (int r = 0; r < 4; ++r) {
+        b.p[i].gsx[r] = gsx[4 * (i0 + i) + r];
+        b.p[i].yv[r] = yv[4 * (i0 + i) + r];
+      }
+    }
+    if (int rc = run_pass1(c, c->geo, y, b, 0, 2, precision, nullptr, nullptr, true)) return rc;
+    if (int rc = run_pass2(c, c->geo, y, b, xunit, 0, 2, precision, 0)) return rc;
+  }
+  return check_launch("hlbl_kernel_sums_batched launch");
+}
+
+int hlbl_ctx_set_batch_group(hlbl_ctx* c, int group) {
+  if (!c || group < 0) return fail(HLBL_EINVAL, "hlbl_ctx_set_batch_group: bad argument");
+  c->batch_group = group;
+  return HLBL_OK;
 }
 
 int hlbl_kernel_sum(hlbl_ctx* c, const double* src, const double* y, const int gsx[4],
@@ -367,6 +537,7 @@ int hlbl_kernel_sum(hlbl_ctx* c, const double* src, const double* y, const int g
   if (e != cudaSuccess) return cuda_fail(e, "result copy");
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "hlbl_kernel_sum");
+  if (int rc = hlbl_ctx_check(c)) return rc;
   out[0] = c->h_out[0];
   out[1] = c->h_out[1];
   return HLBL_OK;
@@ -380,7 +551,8 @@ int hlbl_cu_dzu_dzsu(hlbl_ctx* c, double* d_dzu, double* d_dzsu, const double* s
   if (!aligned16(src) || !aligned16(y)) return fail(HLBL_EINVAL, "hlbl_cu_dzu_dzsu: blocks must be 16-byte aligned");
   Geometry geo{};
   if (int rc = make_geometry(global, local, pc, geo)) return rc;
-  if (int rc = run_pass1(c, geo, src, y, gsx, iflavor, 1, HLBL_FP64, d_dzu, d_dzsu, false)) return rc;
+  PairBatch const b = one_pair(src, nullptr, gsx, nullptr);
+  if (int rc = run_pass1(c, geo, y, b, iflavor, 1, HLBL_FP64, d_dzu, d_dzsu, false)) return rc;
   return check_launch("hlbl_cu_dzu_dzsu launch");
 }
 
@@ -391,7 +563,7 @@ int hlbl_insert_gammas(hlbl_ctx* c, const double* d_dzu, const double* d_dzsu, d
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(c->d_dz + kDzuLen, d_dzsu, (kDzLen - kDzuLen) * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "hlbl_insert_gammas copy");
-  g_build_kernel<<<dim3((kGLen / 2 + 255) / 256, 1), 256, 0, c->stream>>>(c->d_dz, 1, c->d_g);
+  g_build_kernel<<<dim3((kGLen / 2 + 255) / 256, 1, 1), 256, 0, c->stream>>>(c->d_dz, 1, c->d_g);
   e = cudaMemcpyAsync(d_g_dzu, c->d_g, kGDzuLen * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(d_g_dzsu, c->d_g + kGDzuLen, (kGLen - kGDzuLen) * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
@@ -408,9 +580,10 @@ int hlbl_cu_4pt_contraction(hlbl_ctx* c, double* d_ks, const double* d_g_dzu,
   if (!aligned16(src) || !aligned16(y)) return fail(HLBL_EINVAL, "hlbl_cu_4pt_contraction: blocks must be 16-byte aligned");
   Geometry geo{};
   if (int rc = make_geometry(global, local, pc, geo)) return rc;
-  bt_build_kernel<double><<<dim3((kBtK * kBtN + 255) / 256, 1), 256, 0, c->stream>>>(
-      d_g_dzu, d_g_dzsu, 0, 1, static_cast<double*>(c->d_bt));
-  if (int rc = run_pass2(c, geo, src, y, gsx, yv, xunit, iflavor, 1, HLBL_FP64, d_ks, 1)) return rc;
+  bt_build_kernel<double><<<dim3((kBtK * kBtN + 255) / 256, 1, 1), 256, 0, c->stream>>>(
+      d_g_dzu, d_g_dzsu, 0, 0, 1, static_cast<double*>(c->d_bt));
+  PairBatch const b = one_pair(src, d_ks, gsx, yv);
+  if (int rc = run_pass2(c, geo, y, b, xunit, iflavor, 1, HLBL_FP64, 1)) return rc;
   return check_launch("hlbl_cu_4pt_contraction launch");
 }
 
@@ -431,8 +604,9 @@ int hlbl_reserve_kernel_memory(hlbl_ctx* c, size_t* bytes) {
     cudaMemsetAsync(blk, 0, n * sizeof(double), c->stream);
     for (int prec : {HLBL_FP64, HLBL_FP32}) {
       for (int nf : {1, 2}) {
-        run_pass1(c, geo, blk, blk, zero, 0, nf, prec, nullptr, nullptr, true);
-        run_pass2(c, geo, blk, blk, zero, one, 1.0, 0, nf, prec, c->d_out, 0);
+        PairBatch const b = one_pair(blk, c->d_out, zero, one);
+        run_pass1(c, geo, blk, b, 0, nf, prec, nullptr, nullptr, true);
+        run_pass2(c, geo, blk, b, 1.0, 0, nf, prec, 0);
       }
     }
     e = cudaStreamSynchronize(c->stream);
@@ -443,6 +617,157 @@ int hlbl_reserve_kernel_memory(hlbl_ctx* c, size_t* bytes) {
   if (e != cudaSuccess) return cuda_fail(e, "hlbl_reserve_kernel_memory");
   *bytes = free0 > free1 ? free0 - free1 : 0;
   return HLBL_OK;
+}
+
+int hlbl_ctx_reserve(hlbl_ctx* c, int max_pairs) {
+  if (!c || max_pairs < 1) return fail(HLBL_EINVAL, "hlbl_ctx_reserve: bad argument");
+  long long const need = c->geo.V * std::min(max_pairs, kMaxBatch);
+  if (need <= c->w_cap) return HLBL_OK;
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->d_w);
+  c->d_w = nullptr;
+  c->w_cap = 0;
+  cudaError_t e = cudaMalloc(&c->d_w, sizeof(double) * 3 * HLBL_QED_NW * (size_t)need);
+  if (e != cudaSuccess) return fail(HLBL_ENOMEM, "QED weight buffer: %s", cudaGetErrorString(e));
+  c->w_cap = need;
+  return HLBL_OK;
+}
+
+int hlbl_stage_async(hlbl_ctx* c, void* d_dst, const void* h_src, size_t bytes, int after_compute) {
+  if (!c || !d_dst || !h_src) return fail(HLBL_EINVAL, "hlbl_stage_async: null argument");
+  cudaError_t e = cudaSuccess;
+  if (after_compute) {
+    // the destination may still be read by contraction work already enqueued
+    e = cudaEventRecord(c->compute_ev, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, c->compute_ev, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "hlbl_stage_async ordering");
+  }
+  e = cudaMemcpyAsync(d_dst, h_src, bytes, cudaMemcpyHostToDevice, c->copy_stream);
+  if (e == cudaSuccess) e = cudaEventRecord(c->stage_ev, c->copy_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "hlbl_stage_async");
+  c->stage_pending = true;
+  return HLBL_OK;
+}
+
+int hlbl_autotune(hlbl_ctx* c, const double* y, int n, const double* const* srcs, const int* gsx,
+                  const int* yv, double xunit, double* d_out, int* best_p1, int* best_p2,
+                  int* best_group, double* best_ms) {
+  if (!c || n < 1) return fail(HLBL_EINVAL, "hlbl_autotune: bad argument");
+  if (int rc = hlbl_ctx_reserve(c, n)) return rc;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double best = 1e300;
+  int bp1 = 0, bp2 = 0, bg = kMaxBatch;
+  int const groups[] = {1, 2, 4, 8, 16};
+  for (int p1 = 0; p1 < 2; ++p1)
+    for (int p2 = 0; p2 < 2; ++p2)
+      for (int g : groups) {
+        if (g > 1 && g / 2 >= n) continue;
+        c->p1_small = p1;
+        c->p2_small = p2;
+        c->batch_group = g;
+        cudaEventRecord(a, c->stream);
+        int rc = hlbl_kernel_sums_batched(c, y, n, srcs, gsx, yv, xunit, HLBL_FP32, d_out);
+        cudaEventRecord(b, c->stream);
+        cudaError_t e = cudaEventSynchronize(b);
+        if (rc || e != cudaSuccess) {
+          cudaEventDestroy(a);
+          cudaEventDestroy(b);
+          return rc ? rc : cuda_fail(e, "hlbl_autotune");
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms < best) { best = ms; bp1 = p1; bp2 = p2; bg = g; }
+      }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  c->p1_small = bp1;
+  c->p2_small = bp2;
+  c->batch_group = bg;
+  if (best_p1) *best_p1 = bp1;
+  if (best_p2) *best_p2 = bp2;
+  if (best_group) *best_group = bg;
+  if (best_ms) *best_ms = best;
+  return HLBL_OK;
+}
+
+struct hlbl_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t stream = nullptr;
+};
+
+int hlbl_graph_begin(hlbl_ctx* c) {
+  if (!c || c->capturing) return fail(HLBL_ESTATE, "hlbl_graph_begin: no context or already capturing");
+  if (int rc = hlbl_ctx_reserve(c, kMaxBatch)) return rc;
+  if (c->stage_pending) {
+    cudaError_t e = cudaStreamWaitEvent(c->stream, c->stage_ev, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "hlbl_graph_begin");
+    c->stage_pending = false;
+  }
+  cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCapture");
+  c->capturing = true;
+  return HLBL_OK;
+}
+
+int hlbl_graph_end(hlbl_ctx* c, hlbl_graph** out) {
+  if (!c || !out || !c->capturing) return fail(HLBL_ESTATE, "hlbl_graph_end: not capturing");
+  c->capturing = false;
+  hlbl_graph* g = new hlbl_graph();
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g->graph);
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  if (e != cudaSuccess) {
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    return cuda_fail(e, "hlbl_graph_end");
+  }
+  g->stream = c->stream;
+  *out = g;
+  return HLBL_OK;
+}
+
+int hlbl_graph_launch(hlbl_graph* g, void* stream) {
+  if (!g) return fail(HLBL_EINVAL, "hlbl_graph_launch: null graph");
+  cudaError_t e = cudaGraphLaunch(g->exec, stream ? static_cast<cudaStream_t>(stream) : g->stream);
+  return e == cudaSuccess ? HLBL_OK : cuda_fail(e, "cudaGraphLaunch");
+}
+
+void hlbl_graph_destroy(hlbl_graph* g) {
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+}
+
+int hlbl_ctx_set_qed(hlbl_ctx* c, int mode, hlbl_surrogate* s, double r0) {
+  if (!c) return fail(HLBL_EINVAL, "hlbl_ctx_set_qed: null context");
+  if (mode == HLBL_QED_EXACT) {
+    c->qed_mode = mode;
+    c->sur = nullptr;
+    return HLBL_OK;
+  }
+  if (mode != HLBL_QED_SURROGATE || !s) return fail(HLBL_EINVAL, "hlbl_ctx_set_qed: bad mode or null surrogate");
+  if (!c->d_fallback) {
+    cudaError_t e = cudaMalloc(&c->d_fallback, sizeof(unsigned long long));
+    if (e != cudaSuccess) return fail(HLBL_ENOMEM, "hlbl_ctx_set_qed: %s", cudaGetErrorString(e));
+  }
+  cudaError_t e = cudaMemsetAsync(c->d_fallback, 0, sizeof(unsigned long long), c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "hlbl_ctx_set_qed");
+  c->qed_mode = mode;
+  c->sur = s;
+  c->sur_r0 = r0 < 0 ? sur::surrogate_r0(s) : r0;
+  return HLBL_OK;
+}
+
+int hlbl_ctx_qed_fallbacks(hlbl_ctx* c, unsigned long long* n) {
+  if (!c || !n) return fail(HLBL_EINVAL, "hlbl_ctx_qed_fallbacks: null argument");
+  *n = 0;
+  if (!c->d_fallback) return HLBL_OK;
+  cudaError_t e = cudaMemcpyAsync(n, c->d_fallback, sizeof *n, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return e == cudaSuccess ? HLBL_OK : cuda_fail(e, "hlbl_ctx_qed_fallbacks");
 }
 
 int hlbl_ctx_set_profiling(hlbl_ctx* c, int on) {

@@ -21,6 +21,22 @@ constexpr int kGDzuLen = 6912;
 constexpr int kBtK = 288;          // rows of Bt: (p, q, re/im)
 constexpr int kBtN = 160;          // columns of Bt: (j, nu, lambda), j < 10
 
+// Up to kMaxBatch pairs that share the block y (the pairs one new source
+// closes), passed by value as a kernel parameter; a kernel's blockIdx.y is
+// the pair. Partners run over the same tile sequence at the same time, so
+// y's tiles come from HBM about once and from L2 for the others.
+constexpr int kMaxBatch = 16;
+struct PairDesc {
+  const double* src;  // the partner's block (the pair's x = gsx)
+  double* out;        // its two kernel sums (pass 2 reduction target)
+  int gsx[4];
+  int yv[4];
+};
+struct PairBatch {
+  int n;
+  PairDesc p[kMaxBatch];
+};
+
 // Neumaier's compensated FP64 sum: the site-block and volume sums.
 struct Neu {
   double s = 0.0, c = 0.0;
@@ -32,32 +48,47 @@ struct Neu {
   __device__ __forceinline__ double get() const { return s + c; }
 };
 
-// ---------------------------------------------------------------------------
-// Tile loader: rows (which, fl, ia) of the two blocks into shared memory as T.
-// which = 0 reads `a` at flavour fa(fl), which = 1 reads `b` at fb(fl).
-// Sites past V are zero-filled, so they contribute nothing.
+// Input staging: FP64 kernels double-buffer the FP64 tile (TMA into one
+// stage while computing on the other); FP32 kernels keep one FP64 stage and
+// convert each landed tile once into an FP32 copy, then re-use the stage
+// for the next tile's TMA while computing on the copy (an FP64 -> FP32
+// conversion issues on the FP64 pipe, so converting at every use is slow).
 template <typename T, int NF, int TS>
-__device__ __forceinline__ void load_tile(T* __restrict__ s_in, const double* __restrict__ a,
-                                          const double* __restrict__ b, int fa0, int fa_step,
-                                          int fb0, int fb_step, long long V, long long s0) {
+constexpr size_t stage_bytes() {
+  return sizeof(T) == sizeof(double)
+             ? sizeof(double) * (size_t)(2 * 2 * NF * 12 * TS * 24)
+             : sizeof(double) * (size_t)(2 * NF * 12 * TS * 24) + sizeof(float) * (size_t)(2 * NF * 12 * TS * 24);
+}
+
+// TMA staging of one tile: rows (which, fl, ia) of the two blocks, the
+// tile's nvalid sites each (one contiguous run of nvalid*192 bytes per row),
+// into `stage` [2*NF*12][TS][24] doubles; which = 0 reads `a` at flavour
+// fa0 + fa_step*fl, which = 1 reads `b` at fb0 + fb_step*fl. One thread.
+template <int NF, int TS>
+__device__ __forceinline__ void issue_tile(double* stage, uint64_t* bar, const double* a,
+                                           const double* b, int fa0, int fa_step, int fb0,
+                                           int fb_step, long long V, long long s0) {
   constexpr int kRows = 2 * NF * 12;
-  constexpr int kPer = TS * 12;  // double2 per row
   int const nvalid = (int)min((long long)TS, V - s0);
-  for (int idx = threadIdx.x; idx < kRows * kPer; idx += blockDim.x) {
-    int const row = idx / kPer, w = idx - row * kPer;
-    int const which = row / (NF * 12);
-    int const fl = (row / 12) % NF;
-    int const ia = row % 12;
-    int const site = w / 12;
-    double2 v = make_double2(0.0, 0.0);
-    if (site < nvalid) {
-      int const f = which == 0 ? fa0 + fa_step * fl : fb0 + fb_step * fl;
-      const double* base = (which == 0 ? a : b) + ((size_t)(f * 12 + ia) * V + s0) * 24;
-      v = __ldg(reinterpret_cast<const double2*>(base) + w);
-    }
-    T* o = s_in + (size_t)row * TS * 24 + 2 * w;
-    o[0] = (T)v.x;
-    o[1] = (T)v.y;
+  uint32_t const bytes = (uint32_t)nvalid * 192u;
+  mbar_arrive_expect_tx(bar, bytes * kRows);
+  for (int row = 0; row < kRows; ++row) {
+    int const which = row / (NF * 12), fl = (row / 12) % NF, ia = row % 12;
+    int const f = which == 0 ? fa0 + fa_step * fl : fb0 + fb_step * fl;
+    const double* src = (which == 0 ? a : b) + ((size_t)(f * 12 + ia) * V + s0) * 24;
+    bulk_g2s(stage + (size_t)row * TS * 24, src, bytes, bar);
+  }
+}
+
+// Convert a landed FP64 stage into the FP32 compute copy (all threads).
+template <int NF, int TS>
+__device__ __forceinline__ void convert_stage(const double* __restrict__ st, float* __restrict__ cp) {
+  constexpr int kN = 2 * NF * 12 * TS * 24 / 2;
+  const double2* s2 = reinterpret_cast<const double2*>(st);
+  float2* c2 = reinterpret_cast<float2*>(cp);
+  for (int i = threadIdx.x; i < kN; i += blockDim.x) {
+    double2 const v = s2[i];
+    c2[i] = make_float2((float)v.x, (float)v.y);
   }
 }
 
@@ -73,13 +104,19 @@ __device__ __forceinline__ void load_tile(T* __restrict__ s_in, const double* __
 // tile in T, then into FP64 per tile.
 template <typename T, int NF, int TS>
 __global__ void __launch_bounds__(NF * 144)
-p1_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry geo,
-          int4 gsx4, int f0, double* __restrict__ partials) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* s_in = reinterpret_cast<T*>(smem_raw);                       // [2][NF][12][TS][24]
-  int* s_zh = reinterpret_cast<int*>(s_in + 2 * NF * 12 * TS * 24);  // [TS][4]
+p1_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, int f0,
+          double* __restrict__ partials, int* __restrict__ err) {
+  constexpr int kRows = 2 * NF * 12;
+  constexpr size_t kStage = (size_t)kRows * TS * 24;  // doubles per stage
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double* s_stage = reinterpret_cast<double*>(smem_raw);         // [2][kRows][TS][24]
+  int* s_zh = reinterpret_cast<int*>(smem_raw + stage_bytes<T, NF, TS>());  // [TS][4]
+  __shared__ __align__(8) uint64_t s_bar[2];
+  __shared__ int s_fail;
 
-  int const gsx[4] = {gsx4.x, gsx4.y, gsx4.z, gsx4.w};
+  int const pi = blockIdx.y;
+  const double* __restrict__ src = batch.p[pi].src;
+  int const gsx[4] = {batch.p[pi].gsx[0], batch.p[pi].gsx[1], batch.p[pi].gsx[2], batch.p[pi].gsx[3]};
   int const t = threadIdx.x;
   int const fl = t / 144, ia = (t % 144) / 12, ib = t % 12;
 
@@ -87,32 +124,86 @@ p1_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry
   // path, plain on the FP32 path (whose tile sums are only FP32-accurate).
   constexpr bool kComp = sizeof(T) == sizeof(double);
   Neu acc_u[6][2], acc_s[4][2];
+  T tu[6][2], ts[4][2];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) tu[k][0] = tu[k][1] = T(0);
+#pragma unroll
+  for (int s = 0; s < 4; ++s) ts[s][0] = ts[s][1] = T(0);
+  int pending_sites = 0;
+  auto flush = [&]() {
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        if (kComp) acc_u[k][e].add((double)tu[k][e]);
+        else acc_u[k][e].s += (double)tu[k][e];
+        tu[k][e] = T(0);
+      }
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        if (kComp) acc_s[s][e].add((double)ts[s][e]);
+        else acc_s[s][e].s += (double)ts[s][e];
+        ts[s][e] = T(0);
+      }
+    pending_sites = 0;
+  };
 
+  constexpr bool kDB = sizeof(T) == sizeof(double);  // double-buffered FP64 stages
+  float* s_copy = reinterpret_cast<float*>(s_stage + kStage);  // FP32 mode: the converted tile
+  if (t == 0) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    fence_mbar_init();
+    s_fail = 0;
+  }
+  __syncthreads();
   long long const ntiles = (geo.V + TS - 1) / TS;
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  long long tile = blockIdx.x;
+  // src flavour f0+fl, y flavour 1-(f0+fl)
+  if (t == 0 && tile < ntiles) issue_tile<NF, TS>(s_stage, &s_bar[0], src, y, f0, 1, 1 - f0, -1, geo.V, tile * TS);
+  bool next_in_flight = false;
+  int i = 0;
+  for (; tile < ntiles; ++i, tile += gridDim.x) {
+    int const st = kDB ? (i & 1) : 0;
     long long const s0 = tile * TS;
-    __syncthreads();
-    // src flavour f0+fl, y flavour 1-(f0+fl)
-    load_tile<T, NF, TS>(s_in, src, y, f0, 1, 1 - f0, -1, geo.V, s0);
-    for (int s = threadIdx.x; s < TS; s += blockDim.x) {
+    int const nvalid = (int)min((long long)TS, geo.V - s0);
+    next_in_flight = tile + gridDim.x < ntiles;
+    // FP64: prefetch into the other stage (its readers passed the last barrier)
+    if (kDB && t == 0 && next_in_flight) {
+      fence_proxy_async_smem();
+      issue_tile<NF, TS>(s_stage + (st ^ 1) * kStage, &s_bar[st ^ 1], src, y, f0, 1, 1 - f0, -1,
+                         geo.V, (tile + gridDim.x) * TS);
+    }
+    for (int s = t; s < TS; s += blockDim.x) {
       int rel[4];
       rel_coords(geo, gsx, min(s0 + s, geo.V - 1), rel);
-      bool const ok = s0 + s < geo.V;
 #pragma unroll
-      for (int r = 0; r < 4; ++r) s_zh[s * 4 + r] = ok ? coord_map_zerohalf(rel[r], geo.global[r]) : 0;
+      for (int r = 0; r < 4; ++r) s_zh[s * 4 + r] = coord_map_zerohalf(rel[r], geo.global[r]);
     }
+    uint32_t const parity = kDB ? (uint32_t)((i >> 1) & 1) : (uint32_t)(i & 1);
+    if (!mbar_wait(&s_bar[st], parity)) s_fail = 1;
     __syncthreads();
+    if (s_fail) break;
+    const T* tile_data;
+    if constexpr (kDB) {
+      tile_data = reinterpret_cast<const T*>(s_stage + st * kStage);
+    } else {
+      // FP32: convert once, then the stage takes the next tile while we compute
+      convert_stage<NF, TS>(s_stage, s_copy);
+      __syncthreads();
+      if (t == 0 && next_in_flight) {
+        fence_proxy_async_smem();
+        issue_tile<NF, TS>(s_stage, &s_bar[0], src, y, f0, 1, 1 - f0, -1, geo.V, (tile + gridDim.x) * TS);
+      }
+      tile_data = reinterpret_cast<const T*>(s_copy);
+    }
 
-    T tu[6][2], ts[4][2];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) tu[k][0] = tu[k][1] = T(0);
-#pragma unroll
-    for (int s = 0; s < 4; ++s) ts[s][0] = ts[s][1] = T(0);
-
-    const T* A_base = s_in + ((size_t)(0 * NF + fl) * 12 + ia) * TS * 24;
-    const T* B_base = s_in + ((size_t)(1 * NF + fl) * 12 + ib) * TS * 24;
+    const T* A_base = tile_data + ((size_t)(0 * NF + fl) * 12 + ia) * TS * 24;
+    const T* B_base = tile_data + ((size_t)(1 * NF + fl) * 12 + ib) * TS * 24;
 #pragma unroll 1
-    for (int s = 0; s < TS; ++s) {
+    for (int s = 0; s < nvalid; ++s) {
       const T* A = A_base + s * 24;
       const T* B = B_base + s * 24;
       // P[s1][s2] for s2 = s1^2 (gamma_0, gamma_3) and s2 = 3-s1 (gamma_1, gamma_2)
@@ -122,10 +213,10 @@ p1_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry
         T ar = 0, ai = 0, br = 0, bi = 0;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          T const yr = B[2 * (3 * s1 + c)], yi = B[2 * (3 * s1 + c) + 1];
+          T const yr = (T)B[2 * (3 * s1 + c)], yi = (T)B[2 * (3 * s1 + c) + 1];
           int const sa = s1 ^ 2, sb = 3 - s1;
-          T const xr = A[2 * (3 * sa + c)], xi = A[2 * (3 * sa + c) + 1];
-          T const zr = A[2 * (3 * sb + c)], zi = A[2 * (3 * sb + c) + 1];
+          T const xr = (T)A[2 * (3 * sa + c)], xi = (T)A[2 * (3 * sa + c) + 1];
+          T const zr = (T)A[2 * (3 * sb + c)], zi = (T)A[2 * (3 * sb + c) + 1];
           ar += yr * xr + yi * xi;  ai += yr * xi - yi * xr;
           br += yr * zr + yi * zi;  bi += yr * zi - yi * zr;
         }
@@ -137,9 +228,9 @@ p1_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry
         T xr = 0, xi = 0;
 #pragma unroll
         for (int s1 = 0; s1 < 4; ++s1) {
-          T const* p = (sg == 0 || sg == 3) ? pa[s1] : pb[s1];
+          T const* pp = (sg == 0 || sg == 3) ? pa[s1] : pb[s1];
           T vr, vi;
-          mul_iph(g5g_ph(sg, s1), p[0], p[1], vr, vi);
+          mul_iph(g5g_ph(sg, s1), pp[0], pp[1], vr, vi);
           xr += vr; xi += vi;
         }
         X[sg][0] = xr; X[sg][1] = xi;
@@ -155,23 +246,23 @@ p1_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry
         tu[k][1] += wr * X[g][1] - wg * X[r][1];
       }
     }
-#pragma unroll
-    for (int k = 0; k < 6; ++k)
-#pragma unroll
-      for (int e = 0; e < 2; ++e) {
-        if (kComp) acc_u[k][e].add((double)tu[k][e]);
-        else acc_u[k][e].s += (double)tu[k][e];
-      }
-#pragma unroll
-    for (int s = 0; s < 4; ++s)
-#pragma unroll
-      for (int e = 0; e < 2; ++e) {
-        if (kComp) acc_s[s][e].add((double)ts[s][e]);
-        else acc_s[s][e].s += (double)ts[s][e];
-      }
+    pending_sites += nvalid;
+    // FP64 path: every tile; FP32 path: every >= 32 sites
+    if (kComp || pending_sites >= 32) flush();
+    __syncthreads();
+  }
+  flush();
+  if (s_fail) {
+    // a wait gave up: report it, and let no copy into this CTA's shared
+    // memory outlive it (bounded, as everything else)
+    if (t == 0) {
+      if (err) atomicExch(err, kErrWaitTimeout);
+      if (kDB && next_in_flight) mbar_wait(&s_bar[(i + 1) & 1], (uint32_t)(((i + 1) >> 1) & 1));
+    }
+    return;
   }
 
-  double* out = partials + ((size_t)blockIdx.x * NF + fl) * kDzLen;
+  double* out = partials + (((size_t)pi * gridDim.x + blockIdx.x) * NF + fl) * kDzLen;
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
     out[((k * 12 + ia) * 12 + ib) * 2] = acc_u[k][0].get();
@@ -189,9 +280,11 @@ p1_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry
 // add_to[fl][i] += dz (the reference's accumulate-into-caller semantics).
 static __global__ void p1_reduce_kernel(const double* __restrict__ partials, int ncta, int nf,
                                  double* __restrict__ dz, double* add_dzu, double* add_dzsu) {
-  int const fl = blockIdx.y;
+  int const fl = blockIdx.y, pi = blockIdx.z;
   int const i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= kDzLen || fl >= nf) return;
+  partials += (size_t)pi * ncta * nf * kDzLen;
+  dz += (size_t)pi * nf * kDzLen;
   double s = 0.0, c = 0.0;
   for (int b = 0; b < ncta; ++b) {
     double const v = partials[((size_t)b * nf + fl) * kDzLen + i];
@@ -210,9 +303,11 @@ static __global__ void p1_reduce_kernel(const double* __restrict__ partials, int
 // The host gamma insertion of compute_dzu_dzsu (contract.cpp:58-77) on the
 // device: g_dzu[k][mu][ia] = g_mu g5 dzu[k][ia], g_dzsu[s][mu][ia] the same.
 static __global__ void g_build_kernel(const double* __restrict__ dz, int nf, double* __restrict__ g) {
-  int const fl = blockIdx.y;
+  int const fl = blockIdx.y, pi = blockIdx.z;
   int const i = blockIdx.x * blockDim.x + threadIdx.x;  // complex index into g
   if (i >= kGLen / 2 || fl >= nf) return;
+  dz += (size_t)pi * nf * kDzLen;
+  g += (size_t)pi * nf * kGLen;
   // g layout: [j][mu][ia][ib] complex, j < 6 from dzu, else dzsu
   int const ib = i % 12, ia = (i / 12) % 12, mu = (i / 144) % 4, j = i / 576;
   int const sp = ib / 3, cp = ib % 3;
@@ -235,10 +330,13 @@ static __global__ void g_build_kernel(const double* __restrict__ dz, int nf, dou
 // so that Re Tr(D M) = sum_k Dr[k] Bt[k][n] with Dr = (Re D[p][q], Im D[p][q]).
 template <typename T>
 __global__ void bt_build_kernel(const double* __restrict__ g_dzu, const double* __restrict__ g_dzsu,
-                                size_t g_stride, int nf, T* __restrict__ bt) {
-  int const fl = blockIdx.y;
+                                size_t g_stride, size_t g_pstride, int nf, T* __restrict__ bt) {
+  int const fl = blockIdx.y, pi = blockIdx.z;
   int const i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= kBtK * kBtN || fl >= nf) return;
+  g_dzu += (size_t)pi * g_pstride;
+  g_dzsu += (size_t)pi * g_pstride;
+  bt += (size_t)pi * nf * kBtK * kBtN;
   int const k = i / kBtN, n = i % kBtN;
   int const e = k & 1, pq = k >> 1, p = pq / 12, q = pq % 12;
   int const lam = n & 3, nu = (n >> 2) & 3, j = n >> 4;
@@ -267,135 +365,265 @@ __global__ void bt_build_kernel(const double* __restrict__ g_dzu, const double* 
 // K3 = K(x, x-y) and the zerohalf weights:
 //   coef[mu][(k,nu,lam)]   = K1[k][mu][nu][lam] + K2[k][nu][mu][lam] - K3[k][lam][nu][mu]
 //   coef[mu][(6+t,nu,lam)] = sum_k K3[k][lam][nu][mu] (zh_rho_k [sigma_k = t] - zh_sigma_k [rho_k = t]).
-struct P2Args {
-  int gsx[4];
-  int yv[4];
+// One component kerv[k][mu][nu][lam] of the stand-in QED tensor
+// (include/hlbl_gb300_qed.h, hlbl_qed_entry) in the compute type T, from
+// q = (a[4], b[4], w[6]): the kernel's two arguments and its six weights.
+template <typename T>
+__device__ __forceinline__ T qed_entry_t(const T* __restrict__ q, int k, int mu, int nu, int lam) {
+  const T* a = q;
+  const T* b = q + 4;
+  const T* w = q + 8;
+  int const r = comb_rho(k), s = comb_sigma(k);
+  T v = T(0);
+  if (mu == r && nu == s) v += w[0] * a[lam];
+  if (mu == s && nu == r) v -= w[0] * a[lam];
+  if (mu == r && lam == s) v += w[1] * b[nu];
+  if (mu == s && lam == r) v -= w[1] * b[nu];
+  if (nu == r && lam == s) v += w[2] * (a[mu] - b[mu]);
+  if (nu == s && lam == r) v -= w[2] * (a[mu] - b[mu]);
+  if (mu == nu) v += w[3] * (a[r] * b[s] - a[s] * b[r]) * (a[lam] + b[lam]);
+  if (mu == s) v += w[4] * a[r] * b[nu] * b[lam];
+  if (mu == r) v -= w[4] * a[s] * b[nu] * b[lam];
+  if (lam == s) v += w[5] * b[r] * a[mu] * a[nu];
+  if (lam == r) v -= w[5] * b[s] * a[mu] * a[nu];
+  return v;
+}
+constexpr int kQ = 14;  // per (site, evaluation): a[4], b[4], w[6]
+
+// four consecutive elements from shared memory (16-byte aligned)
+__device__ __forceinline__ void lds4(const float* p, float o[4]) {
+  float4 const v = *reinterpret_cast<const float4*>(p);
+  o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+}
+__device__ __forceinline__ void lds4(const double* p, double o[4]) {
+  double2 const u = *reinterpret_cast<const double2*>(p);
+  double2 const v = *reinterpret_cast<const double2*>(p + 2);
+  o[0] = u.x; o[1] = u.y; o[2] = v.x; o[3] = v.y;
+}
+// CW consecutive elements from global memory (read-only path)
+template <int CW>
+__device__ __forceinline__ void ldg_cols(const float* p, float o[CW]) {
+  if constexpr (CW == 2) {
+    float2 const v = __ldg(reinterpret_cast<const float2*>(p));
+    o[0] = v.x; o[1] = v.y;
+  } else {
+#pragma unroll
+    for (int c = 0; c < CW; ++c) o[c] = __ldg(p + c);
+  }
+}
+template <int CW>
+__device__ __forceinline__ void ldg_cols(const double* p, double o[CW]) {
+#pragma unroll
+  for (int c = 0; c < CW; ++c) o[c] = __ldg(p + c);
+}
+
+// ---------------------------------------------------------------------------
+// QED weights: for every local site x the six weight functions of the three
+// kernel evaluations of pass 2 (cuda_lattice.cu:435, :448, :461):
+//   e = 0: K(xm, ym), e = 1: K(ym, xm), e = 2: K(xm, x - y)
+// with xm = coord_map(x - gsx) xunit, ym = coord_map(yv) xunit and x - y the
+// minimum image (:403-426). Exact FP64 stand-in quadrature, one thread per
+// (site, evaluation). w[(site*3 + e)*6 + j].
+struct WArgs {
+  PairBatch batch;
   double xunit;
-  int f0;      // first flavour
   hlbl_qed_params qp;
+};
+
+__device__ __forceinline__ void qed_args(const Geometry& geo, const int gsx[4], const int yv[4],
+                                         double xunit, long long site, int e, double a[4],
+                                         double b[4]) {
+  int rel[4];
+  rel_coords(geo, gsx, site, rel);
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    double const xm = coord_map(rel[r], geo.global[r]) * xunit;
+    double const ym = coord_map(mod_pos(yv[r], geo.global[r]), geo.global[r]) * xunit;
+    double const xmy = coord_map_diff(rel[r], yv[r], geo.global[r]) * xunit;
+    a[r] = e == 1 ? ym : xm;
+    b[r] = e == 0 ? ym : (e == 1 ? xm : xmy);
+  }
+}
+
+static __global__ void qed_weights_exact_kernel(Geometry geo, WArgs args, double* __restrict__ w) {
+  long long const n = geo.V * 3;
+  int const pi = blockIdx.y;
+  int const gsx[4] = {args.batch.p[pi].gsx[0], args.batch.p[pi].gsx[1], args.batch.p[pi].gsx[2], args.batch.p[pi].gsx[3]};
+  int const yv[4] = {args.batch.p[pi].yv[0], args.batch.p[pi].yv[1], args.batch.p[pi].yv[2], args.batch.p[pi].yv[3]};
+  w += (size_t)pi * n * HLBL_QED_NW;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double a[4], b[4], X, c, Y, ww[HLBL_QED_NW];
+    qed_args(geo, gsx, yv, args.xunit, i / 3, (int)(i % 3), a, b);
+    hlbl_qed_invariants(a, b, &X, &c, &Y);
+    hlbl_qed_weights(&args.qp, X, c, Y, ww);
+#pragma unroll
+    for (int j = 0; j < HLBL_QED_NW; ++j) w[i * HLBL_QED_NW + j] = ww[j];
+  }
+}
+
+struct P2Args {
+  double xunit;
+  int f0;                 // first flavour
+  const double* w;        // QED weights [pair][V][3][6] (qed_weights_*_kernel)
 };
 
 template <typename T, int NF, int TS>
 constexpr size_t p2_smem_bytes() {
-  return sizeof(T) * (size_t)(2 * NF * 12 * TS * 24     // inputs
-                              + TS * NF * 4 * kBtK     // D
+  return stage_bytes<T, NF, TS>()                      // input staging
+         + sizeof(T) * (size_t)(TS * NF * 4 * kBtK     // D
                               + TS * 4 * kBtN)         // coef
-         + sizeof(double) * (size_t)(TS * 3 * HLBL_QED_NQ * HLBL_QED_NW  // node terms
-                                     + TS * 3 * HLBL_QED_NW              // weights
-                                     + TS * 12);                         // xm, xmy, xvzh
+         + sizeof(double) * (size_t)(TS * 12)                            // xm, xmy, xvzh
+         + sizeof(T) * (size_t)(TS * 3 * kQ);                            // tensor inputs
 }
 
 template <typename T, int NF, int TS>
 constexpr size_t p1_smem_bytes() {
-  return sizeof(T) * (size_t)(2 * NF * 12 * TS * 24) + sizeof(int) * TS * 4;
+  return stage_bytes<T, NF, TS>() + sizeof(int) * TS * 4;
 }
 
 // The pass-1 variant of hlbl_cu_dzu_dzsu_noalloc: one flavour, FP64, the
 // same tile as the context's FP64 pass 1.
 struct P1NoAllocTraits {
-  static constexpr int kTS = 16;
+  static constexpr int kTS = 8;
   static constexpr int kThreads = 144;
   static constexpr size_t kSmem = p1_smem_bytes<double, 1, kTS>();
 };
 
 template <typename T, int NF, int TS>
 __global__ void __launch_bounds__(NF * 160)
-p2_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry geo,
-          P2Args args, const T* __restrict__ bt, double* __restrict__ partials) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* s_in = reinterpret_cast<T*>(smem_raw);
-  T* s_D = s_in + 2 * NF * 12 * TS * 24;         // [TS][NF][4][288]
+p2_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, P2Args args,
+          const T* __restrict__ bt_all, double* __restrict__ partials, int* __restrict__ err) {
+  constexpr int kRows = 2 * NF * 12;
+  constexpr size_t kStage = (size_t)kRows * TS * 24;  // doubles per input stage
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double* s_stage = reinterpret_cast<double*>(smem_raw);  // FP64 stage(s) (TMA) [+ FP32 copy]
+  T* s_D = reinterpret_cast<T*>(smem_raw + stage_bytes<T, NF, TS>());  // [TS][NF][4][288]
   T* s_coef = s_D + TS * NF * 4 * kBtK;          // [TS][4][160]
-  double* s_node = reinterpret_cast<double*>(s_coef + TS * 4 * kBtN);  // [TS][3][NQ][NW]
-  double* s_w = s_node + TS * 3 * HLBL_QED_NQ * HLBL_QED_NW;           // [TS][3][NW]
-  double* s_vec = s_w + TS * 3 * HLBL_QED_NW;                          // [TS][12]
+  double* s_vec = reinterpret_cast<double*>(s_coef + TS * 4 * kBtN);   // [TS][12]
+  T* s_q = reinterpret_cast<T*>(s_vec + TS * 12);                      // [TS][3][kQ]
 
   int const t = threadIdx.x;
   int const nthr = blockDim.x;
+  int const pi = blockIdx.y;
+  const double* __restrict__ src = batch.p[pi].src;
+  int const gsx[4] = {batch.p[pi].gsx[0], batch.p[pi].gsx[1], batch.p[pi].gsx[2], batch.p[pi].gsx[3]};
+  int const yv[4] = {batch.p[pi].yv[0], batch.p[pi].yv[1], batch.p[pi].yv[2], batch.p[pi].yv[3]};
+  const double* __restrict__ wq = args.w + (size_t)pi * geo.V * 3 * HLBL_QED_NW;
+  const T* __restrict__ bt = bt_all + (size_t)pi * NF * kBtK * kBtN;
   double const xu = args.xunit;
   double ym[4];
 #pragma unroll
-  for (int r = 0; r < 4; ++r) ym[r] = coord_map(mod_pos(args.yv[r], geo.global[r]), geo.global[r]) * xu;
+  for (int r = 0; r < 4; ++r) ym[r] = coord_map(mod_pos(yv[r], geo.global[r]), geo.global[r]) * xu;
+
+  __shared__ __align__(8) uint64_t s_bar[2];
+  __shared__ int s_fail;
+  if (t == 0) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    fence_mbar_init();
+    s_fail = 0;
+  }
+  __syncthreads();
 
   Neu run;  // this thread's compensated FP64 running sum for its flavour
   long long const ntiles = (geo.V + TS - 1) / TS;
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  long long tile = blockIdx.x;
+  constexpr bool kDB = sizeof(T) == sizeof(double);  // double-buffered FP64 stages
+  float* s_copy = reinterpret_cast<float*>(s_stage + kStage);  // FP32 mode: the converted tile
+  // S = src at flavour 1-f, Y = y at flavour f
+  if (t == 0 && tile < ntiles)
+    issue_tile<NF, TS>(s_stage, &s_bar[0], src, y, 1 - args.f0, -1, args.f0, 1, geo.V, tile * TS);
+  bool next_in_flight = false;
+  int it_tile = 0;
+  for (; tile < ntiles; ++it_tile, tile += gridDim.x) {
     long long const s0 = tile * TS;
-    __syncthreads();
-    // S = src at flavour 1-f, Y = y at flavour f
-    load_tile<T, NF, TS>(s_in, src, y, 1 - args.f0, -1, args.f0, 1, geo.V, s0);
-    // QED kernel: node terms of the three evaluations per site
-    for (int it = t; it < TS * 3 * HLBL_QED_NQ; it += nthr) {
-      int const s = it / (3 * HLBL_QED_NQ), e = (it / HLBL_QED_NQ) % 3, i = it % HLBL_QED_NQ;
+    int const st = kDB ? (it_tile & 1) : 0;
+    int const nvalid = (int)min((long long)TS, geo.V - s0);
+    // FP64: prefetch the next tile into the other stage while this one is computed
+    next_in_flight = tile + gridDim.x < ntiles;
+    if (kDB && t == 0 && next_in_flight) {
+      fence_proxy_async_smem();
+      issue_tile<NF, TS>(s_stage + (st ^ 1) * kStage, &s_bar[st ^ 1], src, y, 1 - args.f0, -1,
+                         args.f0, 1, geo.V, (tile + gridDim.x) * TS);
+    }
+    // per site: xm, x - y (minimum image) and the zerohalf weights
+    for (int it = t; it < TS * 4; it += nthr) {
+      int const s = it >> 2, r = it & 3;
       int rel[4];
-      rel_coords(geo, args.gsx, min(s0 + s, geo.V - 1), rel);
-      double xm[4], xmy[4];
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        xm[r] = coord_map(rel[r], geo.global[r]) * xu;
-        xmy[r] = coord_map_diff(rel[r], args.yv[r], geo.global[r]) * xu;
-      }
-      if (e == 0 && i == 0) {
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          s_vec[s * 12 + r] = xm[r];
-          s_vec[s * 12 + 4 + r] = xmy[r];
-          s_vec[s * 12 + 8 + r] = (double)coord_map_zerohalf(rel[r], geo.global[r]);
-        }
-      }
-      const double* a = e == 1 ? ym : xm;
-      const double* b = e == 0 ? ym : (e == 1 ? xm : xmy);
-      double X, c, Y;
-      hlbl_qed_invariants(a, b, &X, &c, &Y);
-      double const u = args.qp.node[i], v = 1.0 - u;
-      double r2 = u * u * X * X + v * v * Y * Y - 2.0 * u * v * X * Y * c;
-      r2 = r2 > 0 ? r2 : 0.0;
-      double const g = args.qp.weight[i] / (1.0 + r2);
-      double const rr = sqrt(r2 + args.qp.lambda * args.qp.lambda);
-      double const h[HLBL_QED_NW] = {1.0, u, v, u * v, u * u, v * v};
-      double* o = s_node + ((s * 3 + e) * HLBL_QED_NQ + i) * HLBL_QED_NW;
-#pragma unroll
-      for (int j = 0; j < HLBL_QED_NW; ++j) o[j] = g * h[j] * exp(-args.qp.mass[j] * rr);
+      rel_coords(geo, gsx, min(s0 + s, geo.V - 1), rel);
+      s_vec[s * 12 + r] = coord_map(rel[r], geo.global[r]) * xu;
+      s_vec[s * 12 + 4 + r] = coord_map_diff(rel[r], yv[r], geo.global[r]) * xu;
+      s_vec[s * 12 + 8 + r] = (double)coord_map_zerohalf(rel[r], geo.global[r]);
     }
     __syncthreads();
-    for (int it = t; it < TS * 3 * HLBL_QED_NW; it += nthr) {
-      int const s = it / (3 * HLBL_QED_NW), e = (it / HLBL_QED_NW) % 3, j = it % HLBL_QED_NW;
-      double acc = 0.0;
-      for (int i = 0; i < HLBL_QED_NQ; ++i) acc += s_node[((s * 3 + e) * HLBL_QED_NQ + i) * HLBL_QED_NW + j];
-      s_w[(s * 3 + e) * HLBL_QED_NW + j] = acc;
+    // the QED tensor's inputs per (site, evaluation), in T:
+    // e = 0: K(x, y), e = 1: K(y, x), e = 2: K(x, x - y)
+    for (int it = t; it < TS * 3 * kQ; it += nthr) {
+      int const se = it / kQ, i = it % kQ, s = se / 3, e = se % 3;
+      const double* xm = s_vec + s * 12;
+      const double* xmy = xm + 4;
+      double v;
+      if (i < 4) v = e == 1 ? ym[i] : xm[i];
+      else if (i < 8) v = e == 0 ? ym[i - 4] : (e == 1 ? xm[i - 4] : xmy[i - 4]);
+      else v = wq[(size_t)(min(s0 + s, geo.V - 1) * 3 + e) * HLBL_QED_NW + (i - 8)];
+      s_q[it] = (T)v;
     }
     __syncthreads();
-    // coefficients (site-dependent, flavour-independent)
+    // coefficients (site-dependent, flavour-independent), in T
     for (int it = t; it < TS * 4 * kBtN; it += nthr) {
       int const s = it / (4 * kBtN), mu = (it / kBtN) % 4, n = it % kBtN;
       int const lam = n & 3, nu = (n >> 2) & 3, j = n >> 4;
-      const double* xm = s_vec + s * 12;
-      const double* xmy = xm + 4;
-      const double* zh = xm + 8;
-      const double* w1 = s_w + (s * 3 + 0) * HLBL_QED_NW;
-      const double* w2 = s_w + (s * 3 + 1) * HLBL_QED_NW;
-      const double* w3 = s_w + (s * 3 + 2) * HLBL_QED_NW;
-      double cf;
+      const T* q1 = s_q + (s * 3 + 0) * kQ;
+      const T* q2 = q1 + kQ;
+      const T* q3 = q2 + kQ;
+      T cf;
       if (j < 6) {
-        cf = hlbl_qed_entry(w1, xm, ym, j, mu, nu, lam) + hlbl_qed_entry(w2, ym, xm, j, nu, mu, lam) -
-             hlbl_qed_entry(w3, xm, xmy, j, lam, nu, mu);
+        cf = qed_entry_t(q1, j, mu, nu, lam) + qed_entry_t(q2, j, nu, mu, lam) -
+             qed_entry_t(q3, j, lam, nu, mu);
       } else {
+        const double* zh = s_vec + s * 12 + 8;
         int const tau = j - 6;
-        cf = 0.0;
+        cf = T(0);
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
           int const r = comb_rho(k), g = comb_sigma(k);
-          double const wgt = (g == tau ? zh[r] : 0.0) - (r == tau ? zh[g] : 0.0);
-          if (wgt != 0.0) cf += wgt * hlbl_qed_entry(w3, xm, xmy, k, lam, nu, mu);
+          if (g == tau) cf += (T)zh[r] * qed_entry_t(q3, k, lam, nu, mu);
+          if (r == tau) cf -= (T)zh[g] * qed_entry_t(q3, k, lam, nu, mu);
         }
       }
-      s_coef[(s * 4 + mu) * kBtN + n] = (s0 + s < geo.V) ? (T)cf : T(0);
+      s_coef[(s * 4 + mu) * kBtN + n] = (s0 + s < geo.V) ? cf : T(0);
     }
-    // D_mu[p][q] for every site and flavour
+    // the tile's blocks
+    uint32_t const parity = kDB ? (uint32_t)((it_tile >> 1) & 1) : (uint32_t)(it_tile & 1);
+    if (!mbar_wait(&s_bar[st], parity)) s_fail = 1;
+    __syncthreads();
+    if (s_fail) break;
+    const T* tile_data;
+    if constexpr (kDB) {
+      tile_data = reinterpret_cast<const T*>(s_stage + st * kStage);
+    } else {
+      // FP32: convert once, then the stage takes the next tile while we compute
+      convert_stage<NF, TS>(s_stage, s_copy);
+      __syncthreads();
+      if (t == 0 && next_in_flight) {
+        fence_proxy_async_smem();
+        issue_tile<NF, TS>(s_stage, &s_bar[0], src, y, 1 - args.f0, -1, args.f0, 1, geo.V,
+                           (tile + gridDim.x) * TS);
+      }
+      tile_data = reinterpret_cast<const T*>(s_copy);
+    }
+    // D_mu[p][q] for every site and flavour (zero past the tile's valid sites)
     for (int it = t; it < TS * NF * 144; it += nthr) {
       int const s = it / (NF * 144), fl = (it / 144) % NF, pq = it % 144, p = pq / 12, q = pq % 12;
-      const T* S = s_in + ((size_t)(0 * NF + fl) * 12 + q) * TS * 24 + s * 24;
-      const T* Y = s_in + ((size_t)(1 * NF + fl) * 12 + p) * TS * 24 + s * 24;
+      const T* S = tile_data + ((size_t)(0 * NF + fl) * 12 + q) * TS * 24 + s * 24;
+      const T* Y = tile_data + ((size_t)(1 * NF + fl) * 12 + p) * TS * 24 + s * 24;
+      if (s >= nvalid) {
+        T* Dz = s_D + ((size_t)(s * NF + fl) * 4) * kBtK + 2 * (p * 12 + q);
+#pragma unroll
+        for (int mu = 0; mu < 4; ++mu) { Dz[mu * kBtK] = T(0); Dz[mu * kBtK + 1] = T(0); }
+        continue;
+      }
       // O[s1][s2] = sum_c Y[s1][c] conj(S[s2][c]) for s2 = s1^2 and 3-s1
       T oa[4][2], ob[4][2];
 #pragma unroll
@@ -403,10 +631,10 @@ p2_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry
         T ar = 0, ai = 0, br = 0, bi = 0;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          T const yr = Y[2 * (3 * s1 + c)], yi = Y[2 * (3 * s1 + c) + 1];
+          T const yr = (T)Y[2 * (3 * s1 + c)], yi = (T)Y[2 * (3 * s1 + c) + 1];
           int const sa = s1 ^ 2, sb = 3 - s1;
-          T const xr = S[2 * (3 * sa + c)], xi = S[2 * (3 * sa + c) + 1];
-          T const zr = S[2 * (3 * sb + c)], zi = S[2 * (3 * sb + c) + 1];
+          T const xr = (T)S[2 * (3 * sa + c)], xi = (T)S[2 * (3 * sa + c) + 1];
+          T const zr = (T)S[2 * (3 * sb + c)], zi = (T)S[2 * (3 * sb + c) + 1];
           ar += yr * xr + yi * xi;  ai += yi * xr - yr * xi;
           br += yr * zr + yi * zi;  bi += yi * zr - yr * zi;
         }
@@ -429,31 +657,67 @@ p2_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry
       }
     }
     __syncthreads();
-    // F = Dr . Bt and the coefficient dot, thread (fl, n)
-    if (t < NF * kBtN) {
-      int const fl = t / kBtN, n = t % kBtN;
-      T acc[TS][4];
+    // F = Dr . Bt and the coefficient dot. Thread (fl, part, column group):
+    // CW adjacent columns n for TS/SPLIT sites and the 4 mu, k in steps of 4
+    // (128-bit shared loads of D, broadcast across the warp).
+    {
+      constexpr int CW = sizeof(T) == 4 ? 2 : 1;
+      constexpr int SPLIT = sizeof(T) == 4 ? 2 : 1;
+      constexpr int TSS = TS / SPLIT;
+      constexpr int NCOL = kBtN / CW;
+      static_assert(SPLIT * NCOL == kBtN, "one flavour's threads cover its columns once");
+      int const fl = t / kBtN, r = t % kBtN;
+      int const part = r / NCOL, n0 = (r % NCOL) * CW;
+      T acc[TSS][4][CW];
 #pragma unroll
-      for (int s = 0; s < TS; ++s)
+      for (int s = 0; s < TSS; ++s)
 #pragma unroll
-        for (int mu = 0; mu < 4; ++mu) acc[s][mu] = T(0);
-      const T* B = bt + (size_t)fl * kBtK * kBtN + n;
-      const T* Db = s_D + (size_t)fl * 4 * kBtK;
-#pragma unroll 4
-      for (int k = 0; k < kBtK; ++k) {
-        T const b = __ldg(B + (size_t)k * kBtN);
+        for (int mu = 0; mu < 4; ++mu)
 #pragma unroll
-        for (int s = 0; s < TS; ++s)
+          for (int c = 0; c < CW; ++c) acc[s][mu][c] = T(0);
+      const T* B = bt + (size_t)fl * kBtK * kBtN + n0;
+      const T* Db = s_D + ((size_t)(part * TSS) * NF + fl) * 4 * kBtK;
+#pragma unroll 2
+      for (int k = 0; k < kBtK; k += 4) {
+        T b[4][CW];
 #pragma unroll
-          for (int mu = 0; mu < 4; ++mu) acc[s][mu] += Db[((size_t)s * NF * 4 + mu) * kBtK + k] * b;
+        for (int kk = 0; kk < 4; ++kk) ldg_cols<CW>(B + (size_t)(k + kk) * kBtN, b[kk]);
+#pragma unroll
+        for (int s = 0; s < TSS; ++s)
+#pragma unroll
+          for (int mu = 0; mu < 4; ++mu) {
+            T d[4];
+            lds4(Db + ((size_t)s * NF * 4 + mu) * kBtK + k, d);
+#pragma unroll
+            for (int c = 0; c < CW; ++c) {
+              // one FMA per product, accumulated in order (no extra add)
+              T a = acc[s][mu][c];
+              a = fma(d[0], b[0][c], a);
+              a = fma(d[1], b[1][c], a);
+              a = fma(d[2], b[2][c], a);
+              a = fma(d[3], b[3][c], a);
+              acc[s][mu][c] = a;
+            }
+          }
       }
-      T part = T(0);
+      T part_sum = T(0);
 #pragma unroll
-      for (int s = 0; s < TS; ++s)
+      for (int s = 0; s < TSS; ++s)
 #pragma unroll
-        for (int mu = 0; mu < 4; ++mu) part += s_coef[(s * 4 + mu) * kBtN + n] * acc[s][mu];
-      run.add(-(double)part);
+        for (int mu = 0; mu < 4; ++mu)
+#pragma unroll
+          for (int c = 0; c < CW; ++c)
+            part_sum += s_coef[((part * TSS + s) * 4 + mu) * kBtN + n0 + c] * acc[s][mu][c];
+      run.add(-(double)part_sum);
     }
+    __syncthreads();  // D, coef and this stage are rewritten in the next iterations
+  }
+  if (s_fail) {
+    if (t == 0) {
+      if (err) atomicExch(err, kErrWaitTimeout);
+      if (kDB && next_in_flight) mbar_wait(&s_bar[(it_tile + 1) & 1], (uint32_t)(((it_tile + 1) >> 1) & 1));
+    }
+    return;
   }
 
   // block reduction per flavour in a fixed order: warp shuffles, then warps
@@ -475,16 +739,18 @@ p2_kernel(const double* __restrict__ src, const double* __restrict__ y, Geometry
     // warps [fl*160/32, (fl+1)*160/32) hold flavour fl (160 = 5 warps)
     Neu s;
     for (int w = t * (kBtN / 32); w < (t + 1) * (kBtN / 32); ++w) { s.add(s_red[w][0]); s.c += s_red[w][1]; }
-    partials[(size_t)blockIdx.x * NF + t] = s.get();
+    partials[((size_t)pi * gridDim.x + blockIdx.x) * NF + t] = s.get();
   }
 }
 
 // out[fl] = sum_cta partials[cta][fl] (fixed order, compensated); if add
 // is set, out[fl] is added to rather than written.
 static __global__ void p2_reduce_kernel(const double* __restrict__ partials, int ncta, int nf,
-                                 double* __restrict__ out, int add) {
-  int const fl = threadIdx.x;
+                                        PairBatch batch, int add) {
+  int const fl = threadIdx.x, pi = blockIdx.x;
   if (fl >= nf) return;
+  double* __restrict__ out = batch.p[pi].out;
+  partials += (size_t)pi * ncta * nf;
   double s = 0.0, c = 0.0;
   for (int b = 0; b < ncta; ++b) {
     double const v = partials[(size_t)b * nf + fl];

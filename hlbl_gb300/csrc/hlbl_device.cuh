@@ -90,6 +90,57 @@ __device__ __forceinline__ void rel_coords(const Geometry& g, const int gsx[4], 
   }
 }
 
+// ---- TMA bulk copies and mbarriers ----------------------------------------
+// Tiles of propagator rows are staged with cp.async.bulk (1-D TMA): one
+// thread issues a copy per contiguous row run and the mbarrier's transaction
+// count tracks the bytes. Every wait is bounded: after kWaitLimit polls the
+// waiter gives up and the kernel reports kErrWaitTimeout through its error
+// flag instead of spinning forever.
+constexpr uint32_t kWaitLimit = 1u << 20;
+constexpr int kErrWaitTimeout = 1;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// order this thread's (and, after a barrier, the CTA's) generic-proxy shared
+// memory accesses before later async-proxy (TMA) writes to the same bytes
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+// global -> shared, `bytes` a multiple of 16, both addresses 16-byte aligned
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for the phase with the given parity to complete.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
 // (rho, sigma) of the six pairs k, cuda_lattice.cu:52-60
 __host__ __device__ constexpr int comb_rho(int k) { return k < 3 ? 0 : (k < 5 ? 1 : 2); }
 __host__ __device__ constexpr int comb_sigma(int k) { return k < 3 ? k + 1 : (k < 5 ? k - 1 : 3); }

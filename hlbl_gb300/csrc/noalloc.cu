@@ -110,8 +110,12 @@ extern "C" int hlbl_cu_dzu_dzsu_noalloc(double* d_dzu, double* d_dzsu, const dou
                     nblocks, HLBL_NOALLOC_MAX_BLOCKS);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // every block writes its whole slot, so nothing has to be cleared first
-  hg::p1_kernel<double, 1, Kernel::kTS><<<nblocks, Kernel::kThreads, Kernel::kSmem, st>>>(
-      fwd_src, fwd_y, geo, make_int4(gsx[0], gsx[1], gsx[2], gsx[3]), iflavor, partials);
+  hg::PairBatch b{};
+  b.n = 1;
+  b.p[0].src = fwd_src;
+  for (int r = 0; r < 4; ++r) b.p[0].gsx[r] = gsx[r];
+  hg::p1_kernel<double, 1, Kernel::kTS><<<dim3(nblocks, 1), Kernel::kThreads, Kernel::kSmem, st>>>(
+      fwd_y, b, geo, iflavor, partials, nullptr);
   noalloc_reduce_kernel<<<(hg::kDzLen + 255) / 256, 256, 0, st>>>(partials, nblocks, d_dzu, d_dzsu);
   e = cudaGetLastError();
   if (e != cudaSuccess) return hg::cuda_fail(e, "hlbl_cu_dzu_dzsu_noalloc launch");

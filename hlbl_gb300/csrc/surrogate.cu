@@ -1,0 +1,941 @@
+// surrogate.cu -- the learned QED weight: an MLP (3 -> 128 -> 128 -> 128 -> 6,
+// SiLU, BF16 weights and activations, FP32 accumulation on the tensor cores
+// via mma.sync m16n8k16) that corrects a coarse 8-node quadrature of the six
+// weight functions of include/hlbl_gb300_qed.h:
+//
+//   w_j(X, c, Y) = base_j(X, c, Y) * exp(sigma_j * net_j(u)),
+//   u = (2X/R - 1, c, 2Y/R - 1), R = the training radius (6.43 m_mu^-1, 12 fm),
+//
+// base_j the same integral as the exact weight with 8 Gauss-Legendre nodes
+// instead of 16, in FP32. The tensor assembly stays exact (pass 2). Inside
+// the fallback radius r0 (|x| < r0 or |y| < r0) the exact FP64 weight is used.
+//
+// Everything the network needs is trained here, on the GPU: the labels come
+// from the exact FP64 weight, the forward and backward passes are this
+// file's BF16 tensor-core GEMMs, the optimiser is Adam on FP32 master weights.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "contract_kernels.cuh"
+#include "hlbl_gb300.h"
+#include "hlbl_gb300_rng.h"
+#include "hlbl_internal.h"
+
+namespace hg {
+namespace sur {
+
+// ---- parameter layout (FP32 master copy) -----------------------------------
+constexpr int H = 128, NIN = 3, NOUT = HLBL_QED_NW;
+constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + H * NIN, OFF_W2 = OFF_B1 + H, OFF_B2 = OFF_W2 + H * H,
+              OFF_W3 = OFF_B2 + H, OFF_B3 = OFF_W3 + H * H, OFF_W4 = OFF_B3 + H,
+              OFF_B4 = OFF_W4 + NOUT * H, NPARAM = OFF_B4 + NOUT;
+static_assert(NPARAM == HLBL_SURROGATE_NPARAM, "parameter count");
+constexpr int WPAD = H + 8;  // BF16 row stride of the resident weights (bank spread)
+
+__constant__ float c_base_node[8];
+__constant__ float c_base_weight[8];
+
+__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float dsilu(float z) {
+  float const s = 1.0f / (1.0f + __expf(-z));
+  return s * (1.0f + z * (1.0f - s));
+}
+
+// The radial envelope of the base's log-residual, M = max(|x|, |y|): the
+// network learns residual / env(M), which is O(1) at every radius (the
+// residual itself runs from ~1e-8 near the origin to ~0.5 at 12 fm). The
+// floor 1e-6 sits just above the base's own FP32 rounding (~1e-7), which
+// the network cannot learn and must not be amplified into its targets.
+__host__ __device__ __forceinline__ double envelope(double M) {
+  double const q = M / (M + 7.8);
+  return q * q * q * q * q + 1e-6;
+}
+
+// The coarse base: the exact weight's integral with 8 nodes, in FP32.
+__device__ __forceinline__ void base_weights(float X, float c, float Y, float lam, float out[NOUT]) {
+#pragma unroll
+  for (int j = 0; j < NOUT; ++j) out[j] = 0.f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    float const u = c_base_node[i], v = 1.f - u;
+    float r2 = u * u * X * X + v * v * Y * Y - 2.f * u * v * X * Y * c;
+    r2 = fmaxf(r2, 0.f);
+    float const g = c_base_weight[i] / (1.f + r2);
+    float const r = sqrtf(r2 + lam * lam);
+    float const h[NOUT] = {1.f, u, v, u * v, u * u, v * v};
+#pragma unroll
+    for (int j = 0; j < NOUT; ++j) out[j] += g * h[j] * __expf(-(0.6f + 0.2f * j) * r);
+  }
+}
+
+// ---- training data -----------------------------------------------------------
+// Sample i: X, Y uniform in [0, R], c uniform in [-1, 1] (counter hash of
+// (seed, i)); features u, target t_j = log(w_exact) - log(base) (FP64 exact).
+__global__ void make_samples_kernel(long long n, uint64_t seed, float R, hlbl_qed_params qp,
+                                    float* __restrict__ feat, float* __restrict__ target) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    uint64_t h = hlbl_rng_hash64(seed * 0x9E3779B97F4A7C15ULL + (uint64_t)i);
+    double const a = (double)(h >> 11) * (1.0 / 9007199254740992.0);
+    h = hlbl_rng_hash64(h);
+    double const b = (double)(h >> 11) * (1.0 / 9007199254740992.0);
+    h = hlbl_rng_hash64(h);
+    double const cc = (double)(h >> 11) * (1.0 / 9007199254740992.0);
+    double const X = a * R, Y = b * R, c = 2.0 * cc - 1.0;
+    double w[NOUT];
+    hlbl_qed_weights(&qp, X, c, Y, w);
+    float bw[NOUT];
+    base_weights((float)X, (float)c, (float)Y, (float)qp.lambda, bw);
+    feat[i * 3 + 0] = (float)(2.0 * X / R - 1.0);
+    feat[i * 3 + 1] = (float)c;
+    feat[i * 3 + 2] = (float)(2.0 * Y / R - 1.0);
+    double const env = envelope(fmax(X, Y));
+#pragma unroll
+    for (int j = 0; j < NOUT; ++j)
+      target[i * NOUT + j] = (float)((log(w[j]) - log((double)bw[j])) / env);
+  }
+}
+
+// ---- a strided BF16 tensor-core GEMM for training ----------------------------
+// C[M][N] = A[M][K] B[K][N]; element (m,k) of A at A[m*sam + k*sak], (k,n) of
+// B at B[k*sbk + n*sbn], all FP32 in global memory and rounded to BF16 when
+// staged; FP32 accumulation (mma.sync m16n8k16). Split-K over gridDim.z
+// writes partial sums P[z][M][N]; gemm_finish adds them in order.
+constexpr int GT_M = 64, GT_N = 64, GT_K = 32, GT_PAD = 8;
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  __nv_bfloat162 const v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2,
+                                         uint32_t a3, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__global__ void __launch_bounds__(128)
+gemm_bf16_kernel(int M, int N, int K, const float* __restrict__ A, long long sam, long long sak,
+                 const float* __restrict__ B, long long sbk, long long sbn, float* __restrict__ P) {
+  __shared__ __align__(16) __nv_bfloat16 sA[GT_M][GT_K + GT_PAD];
+  __shared__ __align__(16) __nv_bfloat16 sB[GT_N][GT_K + GT_PAD];  // [n][k]
+  int const m0 = blockIdx.y * GT_M, n0 = blockIdx.x * GT_N;
+  int const splits = gridDim.z;
+  int const kchunk = (K + splits - 1) / splits;
+  int const kbeg = blockIdx.z * kchunk, kend = min(K, kbeg + kchunk);
+  int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int const wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  int const g = lane >> 2, tq = lane & 3;
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.f;
+
+  for (int k0 = kbeg; k0 < kend; k0 += GT_K) {
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < GT_M * GT_K; idx += blockDim.x) {
+      int const r = idx / GT_K, kk = idx % GT_K;
+      int const m = m0 + r, k = k0 + kk;
+      float const v = (m < M && k < kend) ? A[m * sam + k * sak] : 0.f;
+      sA[r][kk] = __float2bfloat16_rn(v);
+    }
+    for (int idx = threadIdx.x; idx < GT_N * GT_K; idx += blockDim.x) {
+      int const r = idx / GT_K, kk = idx % GT_K;
+      int const n = n0 + r, k = k0 + kk;
+      float const v = (n < N && k < kend) ? B[k * sbk + n * sbn] : 0.f;
+      sB[r][kk] = __float2bfloat16_rn(v);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ks = 0; ks < GT_K; ks += 16) {
+      uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        int const r = wm + i * 16 + g;
+        af[i][0] = *reinterpret_cast<const uint32_t*>(&sA[r][ks + 2 * tq]);
+        af[i][1] = *reinterpret_cast<const uint32_t*>(&sA[r + 8][ks + 2 * tq]);
+        af[i][2] = *reinterpret_cast<const uint32_t*>(&sA[r][ks + 2 * tq + 8]);
+        af[i][3] = *reinterpret_cast<const uint32_t*>(&sA[r + 8][ks + 2 * tq + 8]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        int const c = wn + j * 8 + g;
+        bfr[j][0] = *reinterpret_cast<const uint32_t*>(&sB[c][ks + 2 * tq]);
+        bfr[j][1] = *reinterpret_cast<const uint32_t*>(&sB[c][ks + 2 * tq + 8]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          mma_bf16(acc[i][j], af[i][0], af[i][1], af[i][2], af[i][3], bfr[j][0], bfr[j][1]);
+    }
+  }
+  float* out = P + (size_t)blockIdx.z * M * N;
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        int const m = m0 + wm + i * 16 + g + (e >= 2 ? 8 : 0);
+        int const n = n0 + wn + j * 8 + 2 * tq + (e & 1);
+        if (m < M && n < N) out[(size_t)m * N + n] = acc[i][j][e];
+      }
+}
+
+// C = sum_z P[z] (+ bias[n]) ; then act: 0 none, 1 SiLU (Z kept in C, H in Hout)
+__global__ void gemm_finish_kernel(int M, int N, int splits, const float* __restrict__ P,
+                                   const float* __restrict__ bias, float* __restrict__ C,
+                                   float* __restrict__ Hout) {
+  long long const n_el = (long long)M * N;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_el;
+       i += (long long)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int z = 0; z < splits; ++z) s += P[(size_t)z * n_el + i];
+    if (bias) s += bias[i % N];
+    C[i] = s;
+    if (Hout) Hout[i] = silu(s);
+  }
+}
+
+// first layer (K = 3) on the CUDA cores: Z1 = feat W1^T + b1, H1 = SiLU(Z1)
+__global__ void layer1_kernel(int B, const float* __restrict__ feat, const float* __restrict__ p,
+                              float* __restrict__ Z, float* __restrict__ Hh) {
+  long long const n_el = (long long)B * H;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_el;
+       i += (long long)gridDim.x * blockDim.x) {
+    int const r = (int)(i / H), n = (int)(i % H);
+    const float* w = p + OFF_W1 + n * NIN;
+    float const z = w[0] * feat[r * 3] + w[1] * feat[r * 3 + 1] + w[2] * feat[r * 3 + 2] + p[OFF_B1 + n];
+    Z[i] = z;
+    Hh[i] = silu(z);
+  }
+}
+
+// loss = mean over rows of sum_j (O - T)^2; dO = 2 (O - T) / B. Per-block
+// partial losses (fixed order) into lossp[blockIdx.x].
+__global__ void loss_kernel(int B, const float* __restrict__ O, const float* __restrict__ T,
+                            float* __restrict__ dO, float* __restrict__ lossp) {
+  __shared__ float red[256];
+  float s = 0.f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B * NOUT; i += gridDim.x * blockDim.x) {
+    float const d = O[i] - T[i];
+    dO[i] = 2.f * d / (float)B;
+    s += d * d;
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) lossp[blockIdx.x] = red[0] / (float)B;
+}
+
+// dZ = dH * SiLU'(Z)
+__global__ void dsilu_kernel(long long n, const float* __restrict__ dH, const float* __restrict__ Z,
+                             float* __restrict__ dZ) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    dZ[i] = dH[i] * dsilu(Z[i]);
+}
+
+// db[n] = sum over rows of dZ[r][n] (fixed order)
+__global__ void colsum_kernel(int B, int N, const float* __restrict__ dZ, float* __restrict__ db) {
+  int const n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  float s = 0.f;
+  for (int r = 0; r < B; ++r) s += dZ[(size_t)r * N + n];
+  db[n] = s;
+}
+
+// Adam on the FP32 master parameters.
+__global__ void adam_kernel(int n, float* __restrict__ p, const float* __restrict__ gr,
+                            float* __restrict__ m, float* __restrict__ v, float lr, float b1,
+                            float b2, float eps, float c1, float c2) {
+  int const i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float const g = gr[i];
+  float const mi = b1 * m[i] + (1.f - b1) * g;
+  float const vi = b2 * v[i] + (1.f - b2) * g * g;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// ---- inference, with the weights resident in shared memory -----------------
+struct InferSmem {
+  __nv_bfloat16 w2[H][WPAD];
+  __nv_bfloat16 w3[H][WPAD];
+  __nv_bfloat16 w4[8][WPAD];  // rows 6, 7 zero
+  float w1[H][NIN];
+  float b1[H], b2[H], b3[H], b4[8];
+  float sigma[8];
+  float feat[8][16][4];   // per warp, 16 rows: u0, u1, u2
+  float outv[8][16][8];   // per warp, 16 rows: net outputs
+};
+
+__global__ void pack_weights_kernel(const float* __restrict__ p, __nv_bfloat16* __restrict__ wb) {
+  // wb: w2 [H][WPAD], w3 [H][WPAD], w4 [8][WPAD]
+  int const i = blockIdx.x * blockDim.x + threadIdx.x;
+  int const total = (2 * H + 8) * WPAD;
+  if (i >= total) return;
+  int const row = i / WPAD, col = i % WPAD;
+  float v = 0.f;
+  if (col < H) {
+    if (row < H) v = p[OFF_W2 + row * H + col];
+    else if (row < 2 * H) v = p[OFF_W3 + (row - H) * H + col];
+    else if (row - 2 * H < NOUT) v = p[OFF_W4 + (row - 2 * H) * H + col];
+  }
+  wb[i] = __float2bfloat16_rn(v);
+}
+
+// One warp: 16 rows through the network; activations stay in registers as
+// mma fragments (a layer's accumulator tiles 2t, 2t+1 are the next layer's
+// A tile t). feat[16][4] in, out[16][8] out (shared memory).
+__device__ __forceinline__ void warp_mlp(const InferSmem& S, const float (*feat)[4], float (*out)[8]) {
+  int const lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+  uint32_t act[8][4];  // A fragments of the current activations: 8 k-tiles of 16
+  // layer 1 (K = 3) on the CUDA cores, straight into fragment positions
+#pragma unroll
+  for (int kt = 0; kt < 8; ++kt) {
+    float v[4][2];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int const r = g + ((q & 1) ? 8 : 0);
+      int const cbase = kt * 16 + ((q & 2) ? 8 : 0) + 2 * tq;
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        int const n = cbase + e;
+        float const z = S.w1[n][0] * feat[r][0] + S.w1[n][1] * feat[r][1] + S.w1[n][2] * feat[r][2] + S.b1[n];
+        v[q][e] = silu(z);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) act[kt][q] = pack_bf16(v[q][0], v[q][1]);
+  }
+  // layers 2, 3 (128 -> 128) on the tensor cores
+#pragma unroll
+  for (int layer = 0; layer < 2; ++layer) {
+    const __nv_bfloat16(*W)[WPAD] = layer == 0 ? S.w2 : S.w3;
+    const float* bias = layer == 0 ? S.b2 : S.b3;
+    float acc[16][4];
+#pragma unroll
+    for (int nt = 0; nt < 16; ++nt) {
+      float const b0 = bias[nt * 8 + 2 * tq], b1v = bias[nt * 8 + 2 * tq + 1];
+      acc[nt][0] = b0; acc[nt][1] = b1v; acc[nt][2] = b0; acc[nt][3] = b1v;
+    }
+#pragma unroll
+    for (int kt = 0; kt < 8; ++kt)
+#pragma unroll
+      for (int nt = 0; nt < 16; ++nt) {
+        uint32_t const bb0 = *reinterpret_cast<const uint32_t*>(&W[nt * 8 + g][kt * 16 + 2 * tq]);
+        uint32_t const bb1 = *reinterpret_cast<const uint32_t*>(&W[nt * 8 + g][kt * 16 + 2 * tq + 8]);
+        mma_bf16(acc[nt], act[kt][0], act[kt][1], act[kt][2], act[kt][3], bb0, bb1);
+      }
+#pragma unroll
+    for (int kt = 0; kt < 8; ++kt) {
+      act[kt][0] = pack_bf16(silu(acc[2 * kt][0]), silu(acc[2 * kt][1]));
+      act[kt][1] = pack_bf16(silu(acc[2 * kt][2]), silu(acc[2 * kt][3]));
+      act[kt][2] = pack_bf16(silu(acc[2 * kt + 1][0]), silu(acc[2 * kt + 1][1]));
+      act[kt][3] = pack_bf16(silu(acc[2 * kt + 1][2]), silu(acc[2 * kt + 1][3]));
+    }
+  }
+  // output layer (128 -> 6, padded to 8)
+  float o[4] = {S.b4[2 * tq], S.b4[2 * tq + 1], S.b4[2 * tq], S.b4[2 * tq + 1]};
+#pragma unroll
+  for (int kt = 0; kt < 8; ++kt) {
+    uint32_t const bb0 = *reinterpret_cast<const uint32_t*>(&S.w4[g][kt * 16 + 2 * tq]);
+    uint32_t const bb1 = *reinterpret_cast<const uint32_t*>(&S.w4[g][kt * 16 + 2 * tq + 8]);
+    mma_bf16(o, act[kt][0], act[kt][1], act[kt][2], act[kt][3], bb0, bb1);
+  }
+  out[g][2 * tq] = o[0];
+  out[g][2 * tq + 1] = o[1];
+  out[g + 8][2 * tq] = o[2];
+  out[g + 8][2 * tq + 1] = o[3];
+}
+
+__device__ void load_infer_smem(InferSmem& S, const float* __restrict__ p,
+                                const __nv_bfloat16* __restrict__ wb, const float* __restrict__ sigma) {
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(wb);
+  uint32_t* dst = reinterpret_cast<uint32_t*>(&S.w2[0][0]);
+  int const nwords = (2 * H + 8) * WPAD / 2;
+  for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = src[i];
+  for (int i = threadIdx.x; i < H * NIN; i += blockDim.x) (&S.w1[0][0])[i] = p[OFF_W1 + i];
+  for (int i = threadIdx.x; i < H; i += blockDim.x) {
+    S.b1[i] = p[OFF_B1 + i];
+    S.b2[i] = p[OFF_B2 + i];
+    S.b3[i] = p[OFF_B3 + i];
+  }
+  if (threadIdx.x < 8) {
+    S.b4[threadIdx.x] = threadIdx.x < NOUT ? p[OFF_B4 + threadIdx.x] : 0.f;
+    S.sigma[threadIdx.x] = threadIdx.x < NOUT ? sigma[threadIdx.x] : 0.f;
+  }
+  __syncthreads();
+}
+
+// Net outputs for given feature rows (tests and the validation sweep):
+// out[i][j] = net_j(feat[i]) (before the sigma scaling).
+__global__ void __launch_bounds__(256)
+infer_rows_kernel(int n, const float* __restrict__ feat, const float* __restrict__ p,
+                  const __nv_bfloat16* __restrict__ wb, const float* __restrict__ sigma,
+                  float* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
+  load_infer_smem(S, p, wb, sigma);
+  int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int const nwarps_total = gridDim.x * (blockDim.x >> 5);
+  for (int base = (blockIdx.x * (blockDim.x >> 5) + warp) * 16; base < n; base += nwarps_total * 16) {
+    if (lane < 16) {
+      int const r = base + lane;
+      for (int q = 0; q < 3; ++q) S.feat[warp][lane][q] = r < n ? feat[r * 3 + q] : 0.f;
+    }
+    __syncwarp();
+    warp_mlp(S, S.feat[warp], S.outv[warp]);
+    __syncwarp();
+    if (lane < 16 && base + lane < n)
+      for (int j = 0; j < NOUT; ++j) out[(size_t)(base + lane) * NOUT + j] = S.outv[warp][lane][j];
+    __syncwarp();
+  }
+}
+
+// The surrogate QED weights of pass 2 (drop-in for qed_weights_exact_kernel):
+// row = (site, evaluation); inside the fallback radius, the exact weight.
+__global__ void __launch_bounds__(256)
+qed_weights_surrogate_kernel(Geometry geo, WArgs args, const float* __restrict__ p,
+                             const __nv_bfloat16* __restrict__ wb, const float* __restrict__ sigma,
+                             float R, double r0, double r1, double* __restrict__ w,
+                             unsigned long long* __restrict__ n_fallback) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
+  load_infer_smem(S, p, wb, sigma);
+  int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  long long const n = geo.V * 3;
+  int const pi = blockIdx.y;
+  int const gsx[4] = {args.batch.p[pi].gsx[0], args.batch.p[pi].gsx[1], args.batch.p[pi].gsx[2], args.batch.p[pi].gsx[3]};
+  int const yv[4] = {args.batch.p[pi].yv[0], args.batch.p[pi].yv[1], args.batch.p[pi].yv[2], args.batch.p[pi].yv[3]};
+  w += (size_t)pi * n * HLBL_QED_NW;
+  long long const nwarps_total = (long long)gridDim.x * (blockDim.x >> 5);
+  unsigned long long fb = 0;
+  for (long long base = ((long long)blockIdx.x * (blockDim.x >> 5) + warp) * 16; base < n;
+       base += nwarps_total * 16) {
+    double X = 0, c = 0, Y = 0;
+    long long const row = base + (lane & 15);
+    if (lane < 16) {
+      if (row < n) {
+        double a[4], b[4];
+        qed_args(geo, gsx, yv, args.xunit, row / 3, (int)(row % 3), a, b);
+        hlbl_qed_invariants(a, b, &X, &c, &Y);
+      }
+      S.feat[warp][lane][0] = (float)(2.0 * X / R - 1.0);
+      S.feat[warp][lane][1] = (float)c;
+      S.feat[warp][lane][2] = (float)(2.0 * Y / R - 1.0);
+    }
+    __syncwarp();
+    warp_mlp(S, S.feat[warp], S.outv[warp]);
+    __syncwarp();
+    if (lane < 16 && row < n) {
+      double* o = w + (size_t)row * HLBL_QED_NW;
+      if (fmin(X, Y) < r0 || fmax(X, Y) > r1) {
+        double ex[HLBL_QED_NW];
+        hlbl_qed_weights(&args.qp, X, c, Y, ex);
+        for (int j = 0; j < NOUT; ++j) o[j] = ex[j];
+        ++fb;
+      } else {
+        float bw[NOUT];
+        base_weights((float)X, (float)c, (float)Y, (float)args.qp.lambda, bw);
+        float const env = (float)envelope(fmax(X, Y));
+        for (int j = 0; j < NOUT; ++j)
+          o[j] = (double)(bw[j] * __expf(S.sigma[j] * S.outv[warp][lane][j] * env));
+      }
+    }
+    __syncwarp();
+  }
+  if (n_fallback && lane < 16) {
+    for (int o = 8; o > 0; o >>= 1) fb += __shfl_down_sync(0x0000ffffu, fb, o, 16);
+    if (lane == 0 && fb) atomicAdd(n_fallback, fb);
+  }
+}
+
+size_t infer_smem_bytes() { return sizeof(InferSmem); }
+
+// Validation: per sample min(X, Y), and the largest relative error over the
+// six weights of the base alone and of base x net.
+__global__ void validate_kernel(long long n, const float* __restrict__ feat,
+                                const float* __restrict__ net, const float* __restrict__ sigma,
+                                float R, hlbl_qed_params qp, float* __restrict__ res) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double const X = 0.5 * ((double)feat[i * 3] + 1.0) * R, c = feat[i * 3 + 1];
+    double const Y = 0.5 * ((double)feat[i * 3 + 2] + 1.0) * R;
+    double ex[NOUT];
+    hlbl_qed_weights(&qp, X, c, Y, ex);
+    float bw[NOUT];
+    base_weights((float)X, (float)c, (float)Y, (float)qp.lambda, bw);
+    double eb = 0, en = 0;
+    double const env = envelope(fmax(X, Y));
+    for (int j = 0; j < NOUT; ++j) {
+      double const wn = (double)bw[j] * exp((double)sigma[j] * (double)net[i * NOUT + j] * env);
+      eb = fmax(eb, fabs((double)bw[j] - ex[j]) / ex[j]);
+      en = fmax(en, fabs(wn - ex[j]) / ex[j]);
+    }
+    res[i * 4] = (float)fmin(X, Y);
+    res[i * 4 + 1] = (float)fmax(X, Y);
+    res[i * 4 + 2] = (float)eb;
+    res[i * 4 + 3] = (float)en;
+  }
+}
+
+// per-block sums of t and t^2 over the six targets
+__global__ void moments_kernel(long long n, const float* __restrict__ t, double* __restrict__ part) {
+  double s[2 * NOUT] = {0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    for (int j = 0; j < NOUT; ++j) {
+      double const v = t[i * NOUT + j];
+      s[j] += v;
+      s[NOUT + j] += v * v;
+    }
+  __shared__ double red[256][2 * NOUT];
+  for (int j = 0; j < 2 * NOUT; ++j) red[threadIdx.x][j] = s[j];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < 2 * NOUT; ++j) {
+      double a = 0;
+      for (int k = 0; k < (int)blockDim.x; ++k) a += red[k][j];
+      part[blockIdx.x * 2 * NOUT + j] = a;
+    }
+  }
+}
+
+__global__ void scale_kernel(long long n, float* __restrict__ t, const float* __restrict__ sigma) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n * NOUT;
+       i += (long long)gridDim.x * blockDim.x)
+    t[i] /= sigma[i % NOUT];
+}
+
+}  // namespace sur
+}  // namespace hg
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+using namespace hg;
+using namespace hg::sur;
+
+struct hlbl_surrogate {
+  int device = 0;
+  int nsm = 0;
+  hlbl_qed_params qp{};
+  float R = 6.43f;
+  double r0 = 0.0;  // exact inside: min(|x|, |y|) < r0
+  double r1 = 0.0;  // exact outside: max(|x|, |y|) > r1
+  float h_sigma[NOUT] = {1, 1, 1, 1, 1, 1};
+  float* d_p = nullptr;      // FP32 master parameters
+  float* d_m = nullptr;      // Adam moments
+  float* d_v = nullptr;
+  float* d_g = nullptr;      // gradients
+  float* d_sigma = nullptr;  // output scales [8]
+  __nv_bfloat16* d_wb = nullptr;  // packed BF16 weights for inference
+  long long adam_t = 0;
+  // per-step work buffers for batch size `cap_b`
+  int cap_b = 0;
+  float *Z1 = nullptr, *H1 = nullptr, *Z2 = nullptr, *H2 = nullptr, *Z3 = nullptr, *H3 = nullptr;
+  float *O = nullptr, *dO = nullptr, *dA = nullptr, *dB = nullptr, *P = nullptr, *lossp = nullptr;
+};
+
+namespace {
+
+constexpr int kSplit = 32;
+
+void free_work(hlbl_surrogate* s) {
+  for (float** b : {&s->Z1, &s->H1, &s->Z2, &s->H2, &s->Z3, &s->H3, &s->O, &s->dO, &s->dA, &s->dB,
+                    &s->P, &s->lossp}) {
+    cudaFree(*b);
+    *b = nullptr;
+  }
+  s->cap_b = 0;
+}
+
+int ensure_work(hlbl_surrogate* s, int B) {
+  if (B <= s->cap_b) return HLBL_OK;
+  free_work(s);
+  size_t const bh = (size_t)B * H * sizeof(float);
+  struct { float** p; size_t n; } bufs[] = {
+      {&s->Z1, bh}, {&s->H1, bh}, {&s->Z2, bh}, {&s->H2, bh}, {&s->Z3, bh}, {&s->H3, bh},
+      {&s->O, (size_t)B * NOUT * 4}, {&s->dO, (size_t)B * NOUT * 4}, {&s->dA, bh}, {&s->dB, bh},
+      {&s->P, std::max<size_t>((size_t)kSplit * H * H, (size_t)B * H) * 4 + 4096},
+      {&s->lossp, 4096 * 4}};
+  for (auto& b : bufs) {
+    cudaError_t e = cudaMalloc(b.p, b.n);
+    if (e != cudaSuccess) { free_work(s); return fail(HLBL_ENOMEM, "surrogate work buffer: %s", cudaGetErrorString(e)); }
+  }
+  s->cap_b = B;
+  return HLBL_OK;
+}
+
+// C = A B (+bias, SiLU into Hout) through the tensor-core GEMM
+void gemm(int M, int N, int K, const float* A, long long sam, long long sak, const float* Bm,
+          long long sbk, long long sbn, float* P, int splits, const float* bias, float* C,
+          float* Hout) {
+  dim3 grid((N + GT_N - 1) / GT_N, (M + GT_M - 1) / GT_M, splits);
+  gemm_bf16_kernel<<<grid, 128>>>(M, N, K, A, sam, sak, Bm, sbk, sbn, P);
+  long long const n = (long long)M * N;
+  int const blocks = (int)std::min<long long>((n + 255) / 256, 4096);
+  gemm_finish_kernel<<<blocks, 256>>>(M, N, splits, P, bias, C, Hout);
+}
+
+// One forward + backward over rows [feat, target) of size B: gradients into
+// s->d_g (parameter layout), the loss into *loss (host) if not null.
+int train_step(hlbl_surrogate* s, const float* feat, const float* target, int B, float* loss) {
+  if (int rc = ensure_work(s, B)) return rc;
+  const float* p = s->d_p;
+  float* g = s->d_g;
+  int const eb = (int)std::min<long long>(((long long)B * H + 255) / 256, 4096);
+  // forward
+  layer1_kernel<<<eb, 256>>>(B, feat, p, s->Z1, s->H1);
+  gemm(B, H, H, s->H1, H, 1, p + OFF_W2, 1, H, s->P, 1, p + OFF_B2, s->Z2, s->H2);
+  gemm(B, H, H, s->H2, H, 1, p + OFF_W3, 1, H, s->P, 1, p + OFF_B3, s->Z3, s->H3);
+  gemm(B, NOUT, H, s->H3, H, 1, p + OFF_W4, 1, H, s->P, 1, p + OFF_B4, s->O, nullptr);
+  int const lb = std::min(1024, (B * NOUT + 255) / 256);
+  loss_kernel<<<lb, 256>>>(B, s->O, target, s->dO, s->lossp);
+  // backward
+  gemm(NOUT, H, B, s->dO, 1, NOUT, s->H3, H, 1, s->P, kSplit, nullptr, g + OFF_W4, nullptr);
+  colsum_kernel<<<1, 32>>>(B, NOUT, s->dO, g + OFF_B4);
+  gemm(B, H, NOUT, s->dO, NOUT, 1, p + OFF_W4, H, 1, s->P, 1, nullptr, s->dA, nullptr);  // dH3
+  dsilu_kernel<<<eb, 256>>>((long long)B * H, s->dA, s->Z3, s->dB);                     // dZ3
+  gemm(H, H, B, s->dB, 1, H, s->H2, H, 1, s->P, kSplit, nullptr, g + OFF_W3, nullptr);
+  colsum_kernel<<<1, H>>>(B, H, s->dB, g + OFF_B3);
+  gemm(B, H, H, s->dB, H, 1, p + OFF_W3, H, 1, s->P, 1, nullptr, s->dA, nullptr);        // dH2
+  dsilu_kernel<<<eb, 256>>>((long long)B * H, s->dA, s->Z2, s->dB);                     // dZ2
+  gemm(H, H, B, s->dB, 1, H, s->H1, H, 1, s->P, kSplit, nullptr, g + OFF_W2, nullptr);
+  colsum_kernel<<<1, H>>>(B, H, s->dB, g + OFF_B2);
+  gemm(B, H, H, s->dB, H, 1, p + OFF_W2, H, 1, s->P, 1, nullptr, s->dA, nullptr);        // dH1
+  dsilu_kernel<<<eb, 256>>>((long long)B * H, s->dA, s->Z1, s->dB);                     // dZ1
+  gemm(H, NIN, B, s->dB, 1, H, feat, NIN, 1, s->P, kSplit, nullptr, g + OFF_W1, nullptr);
+  colsum_kernel<<<1, H>>>(B, H, s->dB, g + OFF_B1);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "surrogate train step");
+  if (loss) {
+    std::vector<float> lp(lb);
+    e = cudaMemcpy(lp.data(), s->lossp, lb * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "surrogate loss");
+    double a = 0;
+    for (float v : lp) a += v;
+    *loss = (float)a;
+  }
+  return HLBL_OK;
+}
+
+int pack(hlbl_surrogate* s) {
+  int const total = (2 * H + 8) * WPAD;
+  pack_weights_kernel<<<(total + 255) / 256, 256>>>(s->d_p, s->d_wb);
+  cudaError_t e = cudaMemcpy(s->d_sigma, s->h_sigma, NOUT * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  return e == cudaSuccess ? HLBL_OK : cuda_fail(e, "surrogate pack");
+}
+
+void base_nodes(float node[8], float weight[8]) {
+  // 8-node Gauss-Legendre on [0,1] (Newton on P_8)
+  int const n = 8;
+  double const pi = 3.14159265358979323846;
+  for (int i = 0; i < n; ++i) {
+    double t = std::cos(pi * (i + 0.75) / (n + 0.5)), dp = 1;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1, p1 = t;
+      for (int l = 2; l <= n; ++l) { double p2 = ((2.0 * l - 1) * t * p1 - (l - 1.0) * p0) / l; p0 = p1; p1 = p2; }
+      dp = n * (t * p1 - p0) / (t * t - 1);
+      double const dt = p1 / dp;
+      t -= dt;
+      if (std::fabs(dt) < 1e-16) break;
+    }
+    double p0 = 1, p1 = t;
+    for (int l = 2; l <= n; ++l) { double p2 = ((2.0 * l - 1) * t * p1 - (l - 1.0) * p0) / l; p0 = p1; p1 = p2; }
+    dp = n * (t * p1 - p0) / (t * t - 1);
+    node[i] = (float)(0.5 * (1 - t));
+    weight[i] = (float)(1.0 / ((1 - t * t) * dp * dp));
+  }
+}
+
+}  // namespace
+
+namespace hg {
+namespace sur {
+
+// Pass 2's weights from the surrogate (the launch used by capi.cu).
+int launch_surrogate_weights(const hlbl_surrogate* s, const Geometry& geo, const WArgs& wa,
+                             double r0, double* d_w, unsigned long long* d_fallback,
+                             cudaStream_t st, int nsm) {
+  double const r1 = s->r1 > 0 ? s->r1 : (double)s->R;
+  static bool attr = false;
+  size_t const smem = infer_smem_bytes();
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(qed_weights_surrogate_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(e, "surrogate smem attribute");
+    attr = true;
+  }
+  long long const rows = geo.V * 3;
+  int const blocks = (int)std::max<long long>(
+      1, std::min<long long>((rows + 127) / 128, (long long)nsm * 2 / wa.batch.n));
+  qed_weights_surrogate_kernel<<<dim3(blocks, wa.batch.n), 256, smem, st>>>(geo, wa, s->d_p, s->d_wb, s->d_sigma, s->R,
+                                                          r0, r1, d_w, d_fallback);
+  return HLBL_OK;
+}
+
+double surrogate_r0(const hlbl_surrogate* s) { return s->r0; }
+
+}  // namespace sur
+}  // namespace hg
+
+extern "C" {
+
+int hlbl_surrogate_create(hlbl_surrogate** out, int device, double lambda, uint64_t seed) {
+  if (!out) return fail(HLBL_EINVAL, "hlbl_surrogate_create: null argument");
+  *out = nullptr;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  hlbl_surrogate* s = new hlbl_surrogate();
+  s->device = device;
+  hlbl_qed_params_init(&s->qp, lambda);
+  cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, device);
+  auto bail = [&](int rc) { hlbl_surrogate_destroy(s); return rc; };
+  struct { void** p; size_t n; } bufs[] = {
+      {(void**)&s->d_p, NPARAM * 4}, {(void**)&s->d_m, NPARAM * 4}, {(void**)&s->d_v, NPARAM * 4},
+      {(void**)&s->d_g, NPARAM * 4}, {(void**)&s->d_sigma, 8 * 4},
+      {(void**)&s->d_wb, (size_t)(2 * H + 8) * WPAD * 2}};
+  for (auto& b : bufs) {
+    e = cudaMalloc(b.p, b.n);
+    if (e != cudaSuccess) return bail(fail(HLBL_ENOMEM, "surrogate: %s", cudaGetErrorString(e)));
+  }
+  // Xavier-uniform weights from a counter hash, zero biases
+  std::vector<float> p(NPARAM, 0.f);
+  auto uni = [&](uint64_t i) {
+    return (float)((double)(hlbl_rng_hash64(seed * 0x2545F4914F6CDD1DULL + i) >> 11) *
+                   (1.0 / 9007199254740992.0) * 2.0 - 1.0);
+  };
+  auto fill = [&](int off, int fan_out, int fan_in) {
+    float const a = std::sqrt(6.f / (fan_in + fan_out));
+    for (int i = 0; i < fan_out * fan_in; ++i) p[off + i] = a * uni(off + i);
+  };
+  fill(OFF_W1, H, NIN);
+  fill(OFF_W2, H, H);
+  fill(OFF_W3, H, H);
+  fill(OFF_W4, NOUT, H);
+  e = cudaMemcpy(s->d_p, p.data(), NPARAM * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(s->d_m, 0, NPARAM * 4);
+  if (e == cudaSuccess) e = cudaMemset(s->d_v, 0, NPARAM * 4);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "surrogate init"));
+  float node[8], weight[8];
+  base_nodes(node, weight);
+  e = cudaMemcpyToSymbol(c_base_node, node, sizeof node);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_base_weight, weight, sizeof weight);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "surrogate base nodes"));
+  if (int rc = pack(s)) return bail(rc);
+  e = cudaFuncSetAttribute(infer_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)infer_smem_bytes());
+  if (e != cudaSuccess) return bail(cuda_fail(e, "surrogate smem attribute"));
+  *out = s;
+  return HLBL_OK;
+}
+
+void hlbl_surrogate_destroy(hlbl_surrogate* s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  cudaDeviceSynchronize();
+  free_work(s);
+  cudaFree(s->d_p);
+  cudaFree(s->d_m);
+  cudaFree(s->d_v);
+  cudaFree(s->d_g);
+  cudaFree(s->d_sigma);
+  cudaFree(s->d_wb);
+  delete s;
+}
+
+int hlbl_surrogate_params(hlbl_surrogate* s, float* params, float* sigma, int set) {
+  if (!s || !params) return fail(HLBL_EINVAL, "hlbl_surrogate_params: null argument");
+  cudaSetDevice(s->device);
+  cudaError_t e;
+  if (set) {
+    e = cudaMemcpy(s->d_p, params, NPARAM * 4, cudaMemcpyHostToDevice);
+    if (sigma) std::memcpy(s->h_sigma, sigma, sizeof s->h_sigma);
+    if (e != cudaSuccess) return cuda_fail(e, "hlbl_surrogate_params");
+    return pack(s);
+  }
+  e = cudaMemcpy(params, s->d_p, NPARAM * 4, cudaMemcpyDeviceToHost);
+  if (sigma) std::memcpy(sigma, s->h_sigma, sizeof s->h_sigma);
+  return e == cudaSuccess ? HLBL_OK : cuda_fail(e, "hlbl_surrogate_params");
+}
+
+int hlbl_surrogate_gradients(hlbl_surrogate* s, const float* feat, const float* target, int n,
+                             float* grad, float* loss) {
+  if (!s || !feat || !target || !grad || n < 1) return fail(HLBL_EINVAL, "hlbl_surrogate_gradients: bad argument");
+  cudaSetDevice(s->device);
+  float *df = nullptr, *dt = nullptr;
+  cudaError_t e = cudaMalloc(&df, (size_t)n * NIN * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dt, (size_t)n * NOUT * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(df, feat, (size_t)n * NIN * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dt, target, (size_t)n * NOUT * 4, cudaMemcpyHostToDevice);
+  int rc = e == cudaSuccess ? HLBL_OK : cuda_fail(e, "hlbl_surrogate_gradients");
+  if (!rc) rc = train_step(s, df, dt, n, loss);
+  if (!rc) {
+    e = cudaMemcpy(grad, s->d_g, NPARAM * 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = cuda_fail(e, "hlbl_surrogate_gradients");
+  }
+  cudaFree(df);
+  cudaFree(dt);
+  return rc;
+}
+
+int hlbl_surrogate_eval(hlbl_surrogate* s, const float* feat, int n, float* out) {
+  if (!s || !feat || !out || n < 1) return fail(HLBL_EINVAL, "hlbl_surrogate_eval: bad argument");
+  cudaSetDevice(s->device);
+  float *df = nullptr, *dout = nullptr;
+  cudaError_t e = cudaMalloc(&df, (size_t)n * NIN * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dout, (size_t)n * NOUT * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(df, feat, (size_t)n * NIN * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    int const blocks = std::min((n + 127) / 128, s->nsm * 2);
+    infer_rows_kernel<<<blocks, 256, infer_smem_bytes()>>>(n, df, s->d_p, s->d_wb, s->d_sigma, dout);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, dout, (size_t)n * NOUT * 4, cudaMemcpyDeviceToHost);
+  cudaFree(df);
+  cudaFree(dout);
+  return e == cudaSuccess ? HLBL_OK : cuda_fail(e, "hlbl_surrogate_eval");
+}
+
+int hlbl_surrogate_train(hlbl_surrogate* s, const hlbl_train_config* cfg, hlbl_train_report* rep) {
+  if (!s || !cfg) return fail(HLBL_EINVAL, "hlbl_surrogate_train: null argument");
+  if (cfg->n_samples < cfg->batch || cfg->batch < 64 || cfg->steps < 1 || !(cfg->radius > 0))
+    return fail(HLBL_EINVAL, "hlbl_surrogate_train: bad configuration");
+  cudaSetDevice(s->device);
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0);
+  s->R = cfg->radius;
+  long long const N = cfg->n_samples, NV = cfg->n_valid > 0 ? cfg->n_valid : 0;
+  float *feat = nullptr, *target = nullptr;
+  double* mom = nullptr;
+  cudaError_t e = cudaMalloc(&feat, (size_t)(N + NV) * NIN * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&target, (size_t)(N + NV) * NOUT * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&mom, 1024 * 2 * NOUT * sizeof(double));
+  auto done = [&](int rc) {
+    cudaFree(feat);
+    cudaFree(target);
+    cudaFree(mom);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    return rc;
+  };
+  if (e != cudaSuccess) return done(fail(HLBL_ENOMEM, "surrogate training data: %s", cudaGetErrorString(e)));
+  int const gb = s->nsm * 8;
+  make_samples_kernel<<<gb, 256>>>(N, cfg->seed, cfg->radius, s->qp, feat, target);
+  if (NV)
+    make_samples_kernel<<<gb, 256>>>(NV, cfg->seed ^ 0xA5A5A5A5DEADBEEFULL, cfg->radius, s->qp,
+                                     feat + N * NIN, target + N * NOUT);
+  // output scales: the standard deviation of each target
+  moments_kernel<<<1024, 256>>>(N, target, mom);
+  std::vector<double> hm(1024 * 2 * NOUT);
+  e = cudaMemcpy(hm.data(), mom, hm.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return done(cuda_fail(e, "surrogate moments"));
+  for (int j = 0; j < NOUT; ++j) {
+    double a = 0, b = 0;
+    for (int k = 0; k < 1024; ++k) { a += hm[k * 2 * NOUT + j]; b += hm[k * 2 * NOUT + NOUT + j]; }
+    double const mean = a / N, var = std::max(b / N - mean * mean, 1e-20);
+    s->h_sigma[j] = (float)std::sqrt(var + mean * mean);
+  }
+  e = cudaMemcpy(s->d_sigma, s->h_sigma, NOUT * sizeof(float), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return done(cuda_fail(e, "surrogate sigma"));
+  scale_kernel<<<gb, 256>>>(N, target, s->d_sigma);
+  // Adam with a cosine learning-rate decay to 1% of lr
+  int const B = cfg->batch;
+  long long const nb = N / B;
+  float loss = 0.f;
+  for (int step = 0; step < cfg->steps; ++step) {
+    long long const off = (long long)(step % nb) * B;
+    bool const last = step == cfg->steps - 1;
+    if (int rc = train_step(s, feat + off * NIN, target + off * NOUT, B, last ? &loss : nullptr))
+      return done(rc);
+    ++s->adam_t;
+    float const frac = (float)step / (float)cfg->steps;
+    float const lr = cfg->lr * (0.01f + 0.99f * 0.5f * (1.f + std::cos(3.14159265f * frac)));
+    float const b1 = 0.9f, b2 = 0.999f;
+    float const c1 = 1.f - std::pow(b1, (float)s->adam_t), c2 = 1.f - std::pow(b2, (float)s->adam_t);
+    adam_kernel<<<(NPARAM + 255) / 256, 256>>>(NPARAM, s->d_p, s->d_g, s->d_m, s->d_v, lr, b1, b2,
+                                               1e-8f, c1, c2);
+  }
+  if (int rc = pack(s)) return done(rc);
+  hlbl_train_report r{};
+  r.final_loss = loss;
+  // validation through the inference kernel; the fallback radius is the
+  // largest min(|x|, |y|) at which the network's error still exceeds the bound
+  if (NV) {
+    float *net = nullptr, *res = nullptr;
+    e = cudaMalloc(&net, (size_t)NV * NOUT * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&res, (size_t)NV * 4 * 4);
+    if (e != cudaSuccess) { cudaFree(net); return done(fail(HLBL_ENOMEM, "surrogate validation buffers")); }
+    int const blocks = (int)std::min<long long>((NV + 127) / 128, (long long)s->nsm * 2);
+    infer_rows_kernel<<<blocks, 256, infer_smem_bytes()>>>((int)NV, feat + N * NIN, s->d_p, s->d_wb,
+                                                           s->d_sigma, net);
+    validate_kernel<<<gb, 256>>>(NV, feat + N * NIN, net, s->d_sigma, cfg->radius, s->qp, res);
+    std::vector<float> h(NV * 4);
+    e = cudaMemcpy(h.data(), res, h.size() * 4, cudaMemcpyDeviceToHost);
+    cudaFree(net);
+    cudaFree(res);
+    if (e != cudaSuccess) return done(cuda_fail(e, "surrogate validation"));
+    // The accepted region: r0 <= min(|x|, |y|) and max(|x|, |y|) <= r1.
+    // The network's error grows with M = max(|x|, |y|) (the residual's
+    // envelope). Violations with M < R/10 are origin violations and set r0
+    // (their largest min); the smallest M among the others sets r1.
+    double r0 = 0, r1 = cfg->radius;
+    for (long long i = 0; i < NV; ++i)
+      if (h[i * 4 + 3] > cfg->bound && h[i * 4 + 1] < 0.1 * cfg->radius) r0 = std::max(r0, (double)h[i * 4]);
+    if (r0 > 0) r0 *= 1.0 + 1e-6;
+    for (long long i = 0; i < NV; ++i)
+      if (h[i * 4 + 3] > cfg->bound && h[i * 4] >= r0 && h[i * 4 + 1] >= 0.1 * cfg->radius)
+        r1 = std::min(r1, (double)h[i * 4 + 1]);
+    r1 *= 1.0 - 1e-6;
+    double mb = 0, mn = 0, sb = 0, sn = 0;
+    long long cnt = 0;
+    for (long long i = 0; i < NV; ++i) {
+      if (h[i * 4] < r0 || h[i * 4 + 1] > r1) continue;
+      mb = std::max(mb, (double)h[i * 4 + 2]);
+      mn = std::max(mn, (double)h[i * 4 + 3]);
+      sb += (double)h[i * 4 + 2] * h[i * 4 + 2];
+      sn += (double)h[i * 4 + 3] * h[i * 4 + 3];
+      ++cnt;
+    }
+    r.r0 = r0;
+    r.r1 = r1;
+    r.max_rel_err_base = mb;
+    r.max_rel_err_net = mn;
+    r.rms_rel_err_base = cnt ? std::sqrt(sb / cnt) : 0;
+    r.rms_rel_err_net = cnt ? std::sqrt(sn / cnt) : 0;
+    s->r0 = r0;
+    s->r1 = r1;
+  }
+  cudaEventRecord(t1);
+  e = cudaEventSynchronize(t1);
+  if (e != cudaSuccess) return done(cuda_fail(e, "surrogate training"));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, t0, t1);
+  r.train_seconds = ms * 1e-3;
+  if (rep) *rep = r;
+  return done(HLBL_OK);
+}
+
+}  // extern "C"

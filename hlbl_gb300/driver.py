@@ -1,0 +1,120 @@
+"""The schedule loop of the reference's driver (src/driver.cpp:23-165): solve
+each new source, contract it with its partners, free propagators after
+their last pair. Two pair loops:
+
+  per_pair  Contractor.kernel_sum once per pair, as driver.cpp:104-134 does;
+  batched   one kernel_sums_batched per new source (all pairs it closes share
+            its block), optionally recorded as one CUDA graph per window.
+
+`provider(site, dest)` fills a block for a global site (the reference's
+PropagatorProvider::compute); `contract` is a Contractor (or, in CPU tests,
+any object with the same two methods).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Callable, List, Tuple
+
+from . import schedule as sch
+from .cache import PropagatorCache
+
+
+@dataclass
+class PairResult:
+    """driver.hpp/output.hpp PairResult: x, y (wrapped), y - x, chain, window."""
+    x: tuple
+    y: tuple
+    yv: tuple
+    chain: int
+    window: int
+    kernel_sum: Tuple[float, float] = (0.0, 0.0)
+
+
+@dataclass
+class RunStats:
+    positions_solved: int = 0
+    pairs: int = 0
+    cache_peak: int = 0
+    windows: List[int] = field(default_factory=list)
+
+
+def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cache: PropagatorCache,
+              chain: int = 0, precision=0, batched: bool = False, graphs: bool = False,
+              out_factory=None):
+    """One chain; returns ([PairResult], RunStats). With batched=True,
+    out_factory(n) must return a device buffer of n x 2 doubles."""
+    pending = {}
+    for older, newer, _ in sch.all_pairs(steps):
+        pending[older] = pending.get(older, 0) + 1
+        pending[newer] = pending.get(newer, 0) + 1
+    cache.reset(pending)
+    wrap = lambda p: sch.mod_pos(p, lattice)  # noqa: E731
+    results: List[PairResult] = []
+    stats = RunStats()
+    if batched and cache.residency != "device":
+        raise ValueError("the batched loop needs the device cache (every partner resident)")
+    for st in steps:
+        window_rows = []
+        if not batched:
+            # the reference's order: each source contracted right after its
+            # solve, pair by pair (driver.cpp:104-134); peak 16
+            for src in st.sources:
+                dest = cache.begin_insert(src.position)
+                provider(wrap(src.position), dest)
+                stats.positions_solved += 1
+                cache.end_insert(src.position)
+                if not src.partners:
+                    continue
+                gy = wrap(src.position)
+                d_y = cache.device_ptr(src.position, 0)
+                for q in src.partners:
+                    d_x = cache.device_ptr(q, 1)
+                    gx = wrap(q)
+                    yv = sch.site_map_diff(src.position, q, lattice)
+                    ks = contractor.kernel_sum(d_x, d_y, gx, yv, xunit, precision)
+                    window_rows.append(PairResult(gx, gy, yv, chain, st.index, tuple(ks)))
+                    cache.pair_done(q, src.position)
+                    stats.pairs += 1
+        else:
+            # the window's solves first (the reference's serial order, peak
+            # 30), then one batched call per new source, optionally recorded
+            # as one CUDA graph for the window
+            for src in st.sources:
+                dest = cache.begin_insert(src.position)
+                provider(wrap(src.position), dest)
+                stats.positions_solved += 1
+                cache.end_insert(src.position)
+            calls = []
+            for src in st.sources:
+                if not src.partners:
+                    continue
+                gy = wrap(src.position)
+                xs = [cache.device_ptr(q, 1) for q in src.partners]
+                gxs = [wrap(q) for q in src.partners]
+                yvs = [sch.site_map_diff(src.position, q, lattice) for q in src.partners]
+                rows = [PairResult(g, gy, v, chain, st.index) for g, v in zip(gxs, yvs)]
+                calls.append((cache.device_ptr(src.position, 0), xs, gxs, yvs, rows,
+                              out_factory(len(xs)), src))
+            if graphs:
+                contractor.graph_begin()
+            for d_y, xs, gxs, yvs, _, buf, _ in calls:
+                contractor.kernel_sums_batched(d_y, xs, gxs, yvs, xunit, buf, precision)
+            if graphs:
+                g = contractor.graph_end()
+                g.launch()
+            contractor.check()  # the context's stream is done (and no kernel gave up)
+            for _, _, _, _, rows, buf, src in calls:
+                for r, v in zip(rows, buf.cpu().tolist()):
+                    r.kernel_sum = (v[0], v[1])
+                window_rows.extend(rows)
+                for q in src.partners:
+                    cache.pair_done(q, src.position)
+                    stats.pairs += 1
+            if graphs:
+                g.close()
+        results.extend(window_rows)
+        stats.windows.append(len(window_rows))
+    if cache.size() != 0:
+        raise RuntimeError("run_chain: propagators left in the cache")
+    stats.cache_peak = cache.peak
+    return results, stats

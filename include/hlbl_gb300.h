@@ -52,6 +52,16 @@ const char* hlbl_version(void);
 int hlbl_ctx_create(hlbl_ctx** out, const int global[4], const int local[4],
                     const int proc_coords[4], double lambda, int device);
 void hlbl_ctx_destroy(hlbl_ctx* ctx);
+/* Waits for the context's stream and reports HLBL_ECUDA if a contraction
+ * kernel gave up a bounded wait for a staged tile since the last check (the
+ * sums computed since then are invalid); clears the flag. hlbl_kernel_sum
+ * checks by itself. */
+int hlbl_ctx_check(hlbl_ctx* ctx);
+/* Diagnostic of that path: a kernel whose wait can never complete gives up
+ * after its bounded wait (about a second), sets the flag and returns; the
+ * next hlbl_ctx_check reports it. Nothing faults and the context stays
+ * usable. */
+int hlbl_selftest_wait_timeout(hlbl_ctx* ctx);
 /* Run on `stream` (a cudaStream_t) from now on; NULL restores the context's
  * own stream. */
 int hlbl_ctx_set_stream(hlbl_ctx* ctx, void* stream);
@@ -70,6 +80,53 @@ int hlbl_kernel_sum(hlbl_ctx* ctx, const double* d_fwd_src, const double* d_fwd_
 int hlbl_kernel_sum_async(hlbl_ctx* ctx, const double* d_fwd_src, const double* d_fwd_y,
                           const int gsx[4], const int yv[4], double xunit, int precision,
                           double* d_out);
+
+/* The kernel sums of n pairs that share the block y (the pairs one newly
+ * solved source closes): pair i is (x = gsx[i], y = gsx[i] + yv[i]) with
+ * the partner block srcs[i] (host array of device pointers); both flavours
+ * to d_out[2*i..2*i+1] (device). Pairs run in batched launches of up to 16
+ * (hlbl_ctx_set_batch_group) that read y once for all of them.
+ * Asynchronous on the context's stream; capturable into a CUDA graph.
+ * The per-source batching of the driver's pair loop (src/driver.cpp:104-134),
+ * which calls Contractor::kernel_sum once per pair. */
+int hlbl_kernel_sums_batched(hlbl_ctx* ctx, const double* d_fwd_y, int n,
+                             const double* const* d_fwd_src, const int* gsx, const int* yv,
+                             double xunit, int precision, double* d_out);
+/* Pairs per batched launch (1..16; 0 = 16). */
+int hlbl_ctx_set_batch_group(hlbl_ctx* ctx, int group);
+/* Allocate the per-pair work buffers for batches of max_pairs (<= 16) now,
+ * so that later calls allocate nothing (graph capture needs this). */
+int hlbl_ctx_reserve(hlbl_ctx* ctx, int max_pairs);
+
+/* Host-cache staging (PropagatorCache::device_ptr in host mode,
+ * src/propagator_cache.cpp:52-68, which copies synchronously): copy `bytes`
+ * from pinned host memory to d_dst on the context's side stream; the next
+ * contraction call on the context waits for it, so a block can be staged
+ * while the previous source's pairs are computed. With after_compute set the
+ * copy first waits for all contraction work already enqueued on the
+ * context (d_dst may still be read by it, as a reused staging slot is);
+ * with it clear the caller guarantees that nothing enqueued reads d_dst. */
+int hlbl_stage_async(hlbl_ctx* ctx, void* d_dst, const void* h_src, size_t bytes,
+                     int after_compute);
+
+/* Autotuner: times one batch (FP32 products) under each FP32 tile variant
+ * of pass 1 and pass 2 and each batch group (1, 2, 4, 8, 16 pairs per
+ * launch) and keeps the fastest in the context. Writes the sums of the last
+ * trial to d_out. Blocking. */
+int hlbl_autotune(hlbl_ctx* ctx, const double* d_fwd_y, int n, const double* const* d_fwd_src,
+                  const int* gsx, const int* yv, double xunit, double* d_out, int* best_p1,
+                  int* best_p2, int* best_group, double* best_ms);
+
+/* One CUDA graph per window: every asynchronous call made on the context
+ * between hlbl_graph_begin and hlbl_graph_end (typically one
+ * hlbl_kernel_sums_batched per new source of a window) is recorded, not run;
+ * hlbl_graph_launch replays it. Buffers are reserved for 16-pair batches at
+ * begin. The recorded calls keep their pointers and arguments. */
+typedef struct hlbl_graph hlbl_graph;
+int hlbl_graph_begin(hlbl_ctx* ctx);
+int hlbl_graph_end(hlbl_ctx* ctx, hlbl_graph** out);
+int hlbl_graph_launch(hlbl_graph* graph, void* stream);
+void hlbl_graph_destroy(hlbl_graph* graph);
 
 /* Pass 1 of one flavour, ADDED into d_dzu[6][12][12][2] and
  * d_dzsu[4][12][12][2] (the caller zeroes them first). Same arguments and
@@ -126,6 +183,59 @@ int hlbl_reserve_kernel_memory(hlbl_ctx* ctx, size_t* bytes);
 int hlbl_fill_random_block(hlbl_ctx* ctx, double* d_out, uint64_t seed);
 int hlbl_fill_gaussian_block(hlbl_ctx* ctx, double* d_out, uint64_t seed);
 uint64_t hlbl_source_seed(uint64_t run_seed, const int gsx[4]);
+
+/* ---- the learned QED weight ---------------------------------------------
+ * An MLP (3 -> 128 -> 128 -> 128 -> 6, SiLU, BF16 weights and activations,
+ * FP32 accumulation on the tensor cores) that corrects a coarse 8-node FP32
+ * quadrature of the six weight functions: w_j = base_j exp(sigma_j net_j
+ * env(max(|x|,|y|))), env the radial envelope of the base's log-residual.
+ * Trained on the GPU by the library's own forward/backward kernels on
+ * samples labelled by the exact FP64 weight; the exact tensor assembly is
+ * kept; outside the validated region (min(|x|,|y|) < r0 or max(|x|,|y|) >
+ * r1, units of 1/m_mu) pass 2 uses the exact FP64 weight. No counterpart in the
+ * reference (the task's learned-weight extension). */
+#define HLBL_SURROGATE_NPARAM 34310
+typedef struct hlbl_surrogate hlbl_surrogate;
+typedef struct {
+  long long n_samples; /* training samples, X, Y uniform in [0, radius], c in [-1, 1] */
+  int batch;           /* rows per optimiser step */
+  int steps;           /* Adam steps (cosine learning-rate decay to 1% of lr) */
+  float lr;            /* initial learning rate */
+  uint64_t seed;       /* sample seed */
+  float radius;        /* training radius, units of 1/m_mu (6.43 = 12 fm) */
+  long long n_valid;   /* validation samples (0: no validation, r0 = 0) */
+  double bound;        /* per-weight relative error bound of the accepted region */
+} hlbl_train_config;
+typedef struct {
+  float final_loss;          /* last step's loss (normalised targets) */
+  double max_rel_err_net;    /* validation, outside r0: base x net vs exact */
+  double rms_rel_err_net;
+  double max_rel_err_base;   /* the same for the coarse base alone */
+  double rms_rel_err_base;
+  double r0;                 /* exact inside: min(|x|, |y|) < r0 */
+  double train_seconds;      /* sample generation + training + validation */
+  double r1;                 /* exact outside: max(|x|, |y|) > r1 */
+} hlbl_train_report;
+int hlbl_surrogate_create(hlbl_surrogate** out, int device, double lambda, uint64_t seed);
+void hlbl_surrogate_destroy(hlbl_surrogate* s);
+int hlbl_surrogate_train(hlbl_surrogate* s, const hlbl_train_config* cfg, hlbl_train_report* rep);
+/* Host copies of the FP32 parameters [HLBL_SURROGATE_NPARAM] and the six
+ * output scales: read (set = 0) or write (set = 1). */
+int hlbl_surrogate_params(hlbl_surrogate* s, float* params, float* sigma, int set);
+/* One forward + backward pass on host rows feat[n][3] (normalised inputs)
+ * and targets[n][6] (normalised): gradients of the mean squared error in
+ * the parameter layout, and the loss. The training step, exposed for the
+ * gradient check. */
+int hlbl_surrogate_gradients(hlbl_surrogate* s, const float* feat, const float* target, int n,
+                             float* grad, float* loss);
+/* The inference kernel's raw network outputs for host rows feat[n][3]. */
+int hlbl_surrogate_eval(hlbl_surrogate* s, const float* feat, int n, float* out);
+/* Pass 2's QED weight: HLBL_QED_EXACT, or HLBL_QED_SURROGATE with `s` and
+ * fallback radius r0 (r0 < 0: the radius the training validation chose). */
+int hlbl_ctx_set_qed(hlbl_ctx* ctx, int mode, hlbl_surrogate* s, double r0);
+/* (site, evaluation) rows that pass 2 evaluated exactly inside r0, summed
+ * since the mode was set. */
+int hlbl_ctx_qed_fallbacks(hlbl_ctx* ctx, unsigned long long* n);
 
 /* Measurement hooks. With profiling on, the context times every pass-1 and
  * pass-2 contraction kernel with CUDA events on its launching stream;

@@ -126,6 +126,14 @@ def case_inputs(case):
     return random_block(lat, source_seed(seed, gx)), random_block(lat, source_seed(seed, gy))
 
 
+def pair_rel_err(a, b) -> float:
+    """Relative error of a pair's kernel sum as a 2-vector (both flavours):
+    max |a_f - b_f| / max |b_f|. The bar of the FP32 path: a flavour whose
+    sum nearly cancels is measured against the pair's scale."""
+    a, b = np.asarray(a, dtype=float), np.asarray(b, dtype=float)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
 def rel_err(a, b) -> float:
     a, b = np.asarray(a, dtype=float), np.asarray(b, dtype=float)
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
