@@ -44,11 +44,21 @@ def test_driver_device_host_batched_graphs():
             assert a.kernel_sum == b.kernel_sum  # the same kernels on the same data
         key = lambda r: (r.x, r.y)  # noqa: E731
         ref = {key(r): r.kernel_sum for r in dev}
+        # The batched launches split the sites over other CTAs, so the FP64
+        # rounding differs. Measured at the pair's scale (both flavours as
+        # one vector): a flavour that cancels to ~1e-3 of the pair carries
+        # rounding of the pair's size (the oracle's own compensated and plain
+        # orders differ by 7e-13 relative on such a flavour here).
         for name in ("batched", "graphs"):
             rows = runs[name][0]
             assert len(rows) == n_pairs
             for r in rows:
-                assert S.rel_err(r.kernel_sum, ref[key(r)]) <= 1e-12, name
+                assert S.pair_rel_err(r.kernel_sum, ref[key(r)]) <= 1e-12, name
+        for r in dev:
+            src = S.random_block(lat, S.source_seed(7, r.x))
+            yb = S.random_block(lat, S.source_seed(7, r.y))
+            orc = S.oracle_kernel_sum(src, yb, r.x, r.yv, xu, lat)
+            assert S.pair_rel_err(r.kernel_sum, orc) <= 1e-12
         # a few pairs recomputed directly from freshly generated fields
         for r in (dev[0], dev[len(dev) // 2], dev[-1]):
             d_x = torch.empty(c.block_length, dtype=torch.float64, device="cuda")
