@@ -458,7 +458,7 @@ def main():
         "e2e": {"value": round(pairs_total / e2e_s, 4), "unit": "pairs/s",
                 "h2d_bytes_per_step": int(h2d / max(1, len(timed))),
                 "d2h_bytes_per_step": int(d2h / max(1, len(timed)))},
-        "roofline": {"bound": "hbm", "kernel": f"p2_kernel<float,2,{4 if tune['p2_tile'] == 4 else 8}> (batched)",
+        "roofline": {"bound": "hbm", "kernel": f"pass 2, {tune['p2']} (batched)",
                      "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / peaks["hbm_gbs"], 5),
                      "traffic": (traffic or {}).get("bytes_per_launch"),

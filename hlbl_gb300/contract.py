@@ -163,8 +163,13 @@ class Contractor:
         p1, p2, grp, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
         check(lib.hlbl_autotune(self._h, ptr(d_fwd_y), n, srcs, g, y, C.c_double(xunit), ptr(d_out),
                                 C.byref(p1), C.byref(p2), C.byref(grp), C.byref(ms)))
-        return {"p1_tile": 16 if p1.value else 32, "p2_tile": 4 if p2.value else 8,
+        return {"p1_tile": 4 if p1.value else 8,
+                "p2": ("cuda-core tile 4", "cuda-core tile 2", "tensor-core")[p2.value],
                 "batch_group": grp.value, "ms": ms.value}
+
+    def set_tensor_cores(self, on: bool) -> None:
+        """FP32 two-flavour pass 2 on the tensor cores (default) or the CUDA cores."""
+        check(lib.hlbl_ctx_set_tensor_cores(self._h, 1 if on else 0))
 
     def graph_begin(self) -> None:
         check(lib.hlbl_graph_begin(self._h))

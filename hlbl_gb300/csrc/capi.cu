@@ -13,6 +13,7 @@
 #include "hlbl_gb300.h"
 #include "hlbl_gb300_rng.h"
 #include "hlbl_internal.h"
+#include "p2_tc.h"
 
 namespace {
 
@@ -119,8 +120,8 @@ struct P1Launch {
     return HLBL_OK;
   }
   static void launch(int grid, cudaStream_t st, const double* y, const PairBatch& b,
-                     const Geometry& geo, int f0, double* partials, int* err) {
-    p1_kernel<T, NF, TS><<<dim3(grid, b.n), threads, smem, st>>>(y, b, geo, f0, partials, err);
+                     const Geometry& geo, int f0, double* partials, int* err, float* y32 = nullptr) {
+    p1_kernel<T, NF, TS><<<dim3(grid, b.n), threads, smem, st>>>(y, b, geo, f0, partials, err, y32);
   }
   static long long tiles(long long V) { return (V + TS - 1) / TS; }
 };
@@ -193,6 +194,12 @@ struct hlbl_ctx {
   int grid_p1d2 = 0, grid_p1d1 = 0, grid_p1f2 = 0, grid_p1f1 = 0, grid_p1f2s = 0;
   int grid_p2d2 = 0, grid_p2d1 = 0, grid_p2f2 = 0, grid_p2f1 = 0, grid_p2f2s = 0;
   int p1_small = 0, p2_small = 0;  // FP32 tile variants chosen (autotuner)
+  // FP32 two-flavour pass 2 on the tensor cores (p2_tc.cu); off: CUDA cores
+  int tc = 1;
+  int grid_tc = 0;
+  float* d_x32 = nullptr;     // FP32 tile copies: [1 + pair][f32 block] (y first)
+  size_t x32_floats = 0;
+  float* d_btu = nullptr;     // tensor-core B operand [kMaxBatch][tc_btu_floats_per_pair]
   // staging of host blocks on a side stream (hlbl_stage_async)
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t stage_ev = nullptr;
@@ -255,6 +262,24 @@ int per_pair_grid(int resident, int npairs, long long tiles) {
   return (int)std::min(g, tiles);
 }
 
+bool use_tc(const hlbl_ctx* c, int precision, int nf) { return precision == HLBL_FP32 && nf == 2 && c->tc; }
+
+// FP32 tile copies for y and `npairs` partners (grown outside graph capture).
+int ensure_x32(hlbl_ctx* c, const Geometry& geo, int npairs) {
+  size_t const need = (size_t)(1 + npairs) * f32_block_floats(geo.V);
+  if (need <= c->x32_floats) return HLBL_OK;
+  if (c->capturing) return fail(HLBL_ESTATE, "FP32 tile buffer too small during graph capture");
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->d_x32);
+  c->d_x32 = nullptr;
+  c->x32_floats = 0;
+  cudaError_t e = cudaMalloc(&c->d_x32, sizeof(float) * need);
+  if (e != cudaSuccess) return fail(HLBL_ENOMEM, "FP32 tile buffer (%zu bytes): %s", sizeof(float) * need, cudaGetErrorString(e));
+  c->x32_floats = need;
+  return HLBL_OK;
+}
+float* x32_block(hlbl_ctx* c, const Geometry& geo, int slot) { return c->d_x32 + (size_t)slot * f32_block_floats(geo.V); }
+
 // Pass 1 + reduction + gamma insertion + Bt for the batch's pairs, flavours
 // [f0, f0+nf). Pair i, flavour fl: dz at d_dz + (i*nf + fl)*kDzLen, g at
 // d_g + (i*nf + fl)*kGLen, Bt at d_bt + (i*nf + fl)*kBtK*kBtN.
@@ -266,13 +291,21 @@ int run_pass1(hlbl_ctx* c, const Geometry& geo, const double* y, const PairBatch
     c->stage_pending = false;
   }
   int grid;
+  bool const tcp = use_tc(c, precision, nf) && build_bt;
+  PairBatch bb = b;
+  float* y32 = nullptr;
+  if (tcp) {
+    if (int rc = ensure_x32(c, geo, b.n)) return rc;
+    y32 = x32_block(c, geo, 0);
+    for (int i = 0; i < b.n; ++i) bb.p[i].src32 = x32_block(c, geo, 1 + i);
+  }
   prof_begin(c, 0);
   if (precision == HLBL_FP64) {
     if (nf == 2) { grid = per_pair_grid(c->grid_p1d2, b.n, P1D2::tiles(geo.V)); P1D2::launch(grid, c->stream, y, b, geo, f0, c->d_part1, c->d_err); }
     else { grid = per_pair_grid(c->grid_p1d1, b.n, P1D1::tiles(geo.V)); P1D1::launch(grid, c->stream, y, b, geo, f0, c->d_part1, c->d_err); }
   } else {
-    if (nf == 2 && c->p1_small) { grid = per_pair_grid(c->grid_p1f2s, b.n, P1F2s::tiles(geo.V)); P1F2s::launch(grid, c->stream, y, b, geo, f0, c->d_part1, c->d_err); }
-    else if (nf == 2) { grid = per_pair_grid(c->grid_p1f2, b.n, P1F2::tiles(geo.V)); P1F2::launch(grid, c->stream, y, b, geo, f0, c->d_part1, c->d_err); }
+    if (nf == 2 && c->p1_small) { grid = per_pair_grid(c->grid_p1f2s, b.n, P1F2s::tiles(geo.V)); P1F2s::launch(grid, c->stream, y, bb, geo, f0, c->d_part1, c->d_err, y32); }
+    else if (nf == 2) { grid = per_pair_grid(c->grid_p1f2, b.n, P1F2::tiles(geo.V)); P1F2::launch(grid, c->stream, y, bb, geo, f0, c->d_part1, c->d_err, y32); }
     else { grid = per_pair_grid(c->grid_p1f1, b.n, P1F1::tiles(geo.V)); P1F1::launch(grid, c->stream, y, b, geo, f0, c->d_part1, c->d_err); }
   }
   prof_end(c, 0);
@@ -281,7 +314,9 @@ int run_pass1(hlbl_ctx* c, const Geometry& geo, const double* y, const PairBatch
   if (!build_bt) return HLBL_OK;
   g_build_kernel<<<dim3((kGLen / 2 + 255) / 256, nf, b.n), 256, 0, c->stream>>>(c->d_dz, nf, c->d_g);
   dim3 const gb((kBtK * kBtN + 255) / 256, nf, b.n);
-  if (precision == HLBL_FP64)
+  if (tcp)
+    tc_launch_btu(c->d_g, b.n, c->d_btu, c->stream);
+  else if (precision == HLBL_FP64)
     bt_build_kernel<double><<<gb, 256, 0, c->stream>>>(c->d_g, c->d_g + kGDzuLen, kGLen,
                                                        (size_t)nf * kGLen, nf, static_cast<double*>(c->d_bt));
   else
@@ -330,6 +365,15 @@ int run_pass2(hlbl_ctx* c, const Geometry& geo, const double* y, const PairBatch
     const double* bt = static_cast<const double*>(c->d_bt);
     if (nf == 2) { grid = per_pair_grid(c->grid_p2d2, b.n, P2D2::tiles(geo.V)); P2D2::launch(grid, c->stream, y, b, geo, a, bt, c->d_part2, c->d_err); }
     else { grid = per_pair_grid(c->grid_p2d1, b.n, P2D1::tiles(geo.V)); P2D1::launch(grid, c->stream, y, b, geo, a, bt, c->d_part2, c->d_err); }
+  } else if (use_tc(c, precision, nf)) {
+    TcBatch tb{};
+    tb.y32 = x32_block(c, geo, 0);
+    for (int i = 0; i < b.n; ++i) {
+      tb.x32[i] = x32_block(c, geo, 1 + i);
+      for (int r = 0; r < 4; ++r) { tb.gsx[i][r] = b.p[i].gsx[r]; tb.yv[i][r] = b.p[i].yv[r]; }
+    }
+    grid = per_pair_grid(c->grid_tc, b.n, tc_tiles(geo.V));
+    tc_launch_p2(grid, b.n, c->stream, tb, geo, a, c->d_btu, c->d_part2, c->d_err);
   } else {
     const float* bt = static_cast<const float*>(c->d_bt);
     if (nf == 2 && c->p2_small) { grid = per_pair_grid(c->grid_p2f2s, b.n, P2F2s::tiles(geo.V)); P2F2s::launch(grid, c->stream, y, b, geo, a, bt, c->d_part2, c->d_err); }
@@ -391,10 +435,12 @@ int hlbl_ctx_create(hlbl_ctx** out, const int global[4], const int local[4],
       (rc = P1F2::init(c->nsm, c->grid_p1f2)) || (rc = P1F1::init(c->nsm, c->grid_p1f1)) ||
       (rc = P2D2::init(c->nsm, c->grid_p2d2)) || (rc = P2D1::init(c->nsm, c->grid_p2d1)) ||
       (rc = P2F2::init(c->nsm, c->grid_p2f2)) || (rc = P2F1::init(c->nsm, c->grid_p2f1)) ||
-      (rc = P1F2s::init(c->nsm, c->grid_p1f2s)) || (rc = P2F2s::init(c->nsm, c->grid_p2f2s)))
+      (rc = P1F2s::init(c->nsm, c->grid_p1f2s)) || (rc = P2F2s::init(c->nsm, c->grid_p2f2s)) ||
+      (rc = tc_init(c->nsm, c->grid_tc)))
     return bail(rc);
   c->max_grid = std::max({c->grid_p1d2, c->grid_p1d1, c->grid_p1f2, c->grid_p1f1, c->grid_p2d2,
-                          c->grid_p2d1, c->grid_p2f2, c->grid_p2f1, c->grid_p1f2s, c->grid_p2f2s});
+                          c->grid_p2d1, c->grid_p2f2, c->grid_p2f1, c->grid_p1f2s, c->grid_p2f2s,
+                          c->grid_tc});
   e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->stage_ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->compute_ev, cudaEventDisableTiming);
@@ -411,6 +457,7 @@ int hlbl_ctx_create(hlbl_ctx** out, const int global[4], const int local[4],
       {(void**)&c->d_dz, sizeof(double) * kMaxBatch * 2 * kDzLen},
       {(void**)&c->d_g, sizeof(double) * kMaxBatch * 2 * kGLen},
       {(void**)&c->d_bt, sizeof(double) * kMaxBatch * 2 * kBtK * kBtN},
+      {(void**)&c->d_btu, sizeof(float) * kMaxBatch * tc_btu_floats_per_pair()},
       {(void**)&c->d_out, sizeof(double) * 2},
       {(void**)&c->d_err, sizeof(int)}};
   for (auto& b : bufs) {
@@ -434,6 +481,8 @@ void hlbl_ctx_destroy(hlbl_ctx* c) {
   cudaFree(c->d_dz);
   cudaFree(c->d_g);
   cudaFree(c->d_bt);
+  cudaFree(c->d_btu);
+  cudaFree(c->d_x32);
   cudaFree(c->d_out);
   cudaFree(c->d_err);
   cudaFree(c->d_w);
@@ -521,6 +570,12 @@ int hlbl_kernel_sums_batched(hlbl_ctx* c, const double* y, int n, const double* 
     if (int rc = run_pass2(c, c->geo, y, b, xunit, 0, 2, precision, 0)) return rc;
   }
   return check_launch("hlbl_kernel_sums_batched launch");
+}
+
+int hlbl_ctx_set_tensor_cores(hlbl_ctx* c, int on) {
+  if (!c) return fail(HLBL_EINVAL, "hlbl_ctx_set_tensor_cores: null context");
+  c->tc = on ? 1 : 0;
+  return HLBL_OK;
 }
 
 int hlbl_ctx_set_batch_group(hlbl_ctx* c, int group) {
@@ -621,6 +676,10 @@ int hlbl_reserve_kernel_memory(hlbl_ctx* c, size_t* bytes) {
 
 int hlbl_ctx_reserve(hlbl_ctx* c, int max_pairs) {
   if (!c || max_pairs < 1) return fail(HLBL_EINVAL, "hlbl_ctx_reserve: bad argument");
+  if (c->tc) {
+    int const group = c->batch_group > 0 ? std::min(c->batch_group, kMaxBatch) : kMaxBatch;
+    if (int rc = ensure_x32(c, c->geo, std::min(max_pairs, group))) return rc;
+  }
   long long const need = c->geo.V * std::min(max_pairs, kMaxBatch);
   if (need <= c->w_cap) return HLBL_OK;
   cudaStreamSynchronize(c->stream);
@@ -661,12 +720,19 @@ int hlbl_autotune(hlbl_ctx* c, const double* y, int n, const double* const* srcs
   int bp1 = 0, bp2 = 0, bg = kMaxBatch;
   int const groups[] = {1, 2, 4, 8, 16};
   for (int p1 = 0; p1 < 2; ++p1)
-    for (int p2 = 0; p2 < 2; ++p2)
+    for (int p2 = 0; p2 < 3; ++p2)
       for (int g : groups) {
         if (g > 1 && g / 2 >= n) continue;
         c->p1_small = p1;
-        c->p2_small = p2;
+        c->p2_small = p2 == 1;
+        c->tc = p2 == 2;
         c->batch_group = g;
+        if (c->tc)
+          if (int rc = ensure_x32(c, c->geo, std::min(g, n))) {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+            return rc;
+          }
         cudaEventRecord(a, c->stream);
         int rc = hlbl_kernel_sums_batched(c, y, n, srcs, gsx, yv, xunit, HLBL_FP32, d_out);
         cudaEventRecord(b, c->stream);
@@ -683,7 +749,8 @@ int hlbl_autotune(hlbl_ctx* c, const double* y, int n, const double* const* srcs
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   c->p1_small = bp1;
-  c->p2_small = bp2;
+  c->p2_small = bp2 == 1;
+  c->tc = bp2 == 2;
   c->batch_group = bg;
   if (best_p1) *best_p1 = bp1;
   if (best_p2) *best_p2 = bp2;

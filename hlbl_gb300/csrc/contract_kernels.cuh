@@ -29,6 +29,7 @@ constexpr int kMaxBatch = 16;
 struct PairDesc {
   const double* src;  // the partner's block (the pair's x = gsx)
   double* out;        // its two kernel sums (pass 2 reduction target)
+  float* src32;       // FP32 path: pass 1 writes the block's FP32 tile copy here (or null)
   int gsx[4];
   int yv[4];
 };
@@ -92,6 +93,30 @@ __device__ __forceinline__ void convert_stage(const double* __restrict__ st, flo
   }
 }
 
+// Write a converted tile's rows into the FP32 tile copies ([f][ia][tile32]
+// [6][32][4] floats, 32-site tiles): rows of `a` (flavour f0 + fl) into a32,
+// rows of `b` (flavour 1 - f0 - fl) into b32; consecutive threads write
+// consecutive 16-byte groups of one row.
+template <int NF, int TS>
+__device__ __forceinline__ void write_f32_tiles(const float* __restrict__ cp, float* __restrict__ a32,
+                                                float* __restrict__ b32, int f0, long long V, long long s0,
+                                                int nvalid) {
+  static_assert(32 % TS == 0, "a tile lies inside one 32-site tile of the copy");
+  if (a32 == nullptr && b32 == nullptr) return;
+  long long const nt32 = (V + 31) / 32;
+  int const n = 2 * NF * 12 * 6 * nvalid;
+  for (int it = threadIdx.x; it < n; it += blockDim.x) {
+    int const s = it % nvalid, rem = it / nvalid, c4 = rem % 6, row = rem / 6;
+    int const which = row / (NF * 12), fl = (row / 12) % NF, ia = row % 12;
+    float* dst = which == 0 ? a32 : b32;
+    if (dst == nullptr) continue;
+    int const f = which == 0 ? f0 + fl : 1 - f0 - fl;
+    long long const v = s0 + s;
+    size_t const off = ((size_t)(f * 12 + ia) * nt32 + (size_t)(v >> 5)) * (32 * 24) + c4 * 128 + (v & 31) * 4;
+    *reinterpret_cast<float4*>(dst + off) = *reinterpret_cast<const float4*>(cp + ((size_t)row * TS + s) * 24 + c4 * 4);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Pass 1 (ker_dzu_dzsu, cuda_lattice.cu:160-262), per CTA partial sums.
 // Thread (fl, ia, ib) owns dzu[k][ia][ib] and dzsu[s][ia][ib] of flavour
@@ -102,10 +127,13 @@ __device__ __forceinline__ void convert_stage(const double* __restrict__ st, flo
 //   P[s1][s2] = sum_c conj(B[s1][c]) A[s2][c],  s2 = src(s, s1),
 // which is all of g5 g_s's support. Per-site products in T, accumulated per
 // tile in T, then into FP64 per tile.
+// FP32 path: as it converts a tile, pass 1 also writes it into the FP32
+// tile copies the tensor-core pass 2 reads (y32 by pair 0's CTAs, each
+// partner's by its own; null pointers: no copy).
 template <typename T, int NF, int TS>
 __global__ void __launch_bounds__(NF * 144)
 p1_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, int f0,
-          double* __restrict__ partials, int* __restrict__ err) {
+          double* __restrict__ partials, int* __restrict__ err, float* __restrict__ y32) {
   constexpr int kRows = 2 * NF * 12;
   constexpr size_t kStage = (size_t)kRows * TS * 24;  // doubles per stage
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -198,6 +226,7 @@ p1_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, int f0,
         issue_tile<NF, TS>(s_stage, &s_bar[0], src, y, f0, 1, 1 - f0, -1, geo.V, (tile + gridDim.x) * TS);
       }
       tile_data = reinterpret_cast<const T*>(s_copy);
+      write_f32_tiles<NF, TS>(s_copy, batch.p[pi].src32, pi == 0 ? y32 : nullptr, f0, geo.V, s0, nvalid);
     }
 
     const T* A_base = tile_data + ((size_t)(0 * NF + fl) * 12 + ia) * TS * 24;

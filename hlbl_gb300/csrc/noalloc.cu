@@ -115,7 +115,7 @@ extern "C" int hlbl_cu_dzu_dzsu_noalloc(double* d_dzu, double* d_dzsu, const dou
   b.p[0].src = fwd_src;
   for (int r = 0; r < 4; ++r) b.p[0].gsx[r] = gsx[r];
   hg::p1_kernel<double, 1, Kernel::kTS><<<dim3(nblocks, 1), Kernel::kThreads, Kernel::kSmem, st>>>(
-      fwd_y, b, geo, iflavor, partials, nullptr);
+      fwd_y, b, geo, iflavor, partials, nullptr, nullptr);
   noalloc_reduce_kernel<<<(hg::kDzLen + 255) / 256, 256, 0, st>>>(partials, nblocks, d_dzu, d_dzsu);
   e = cudaGetLastError();
   if (e != cudaSuccess) return hg::cuda_fail(e, "hlbl_cu_dzu_dzsu_noalloc launch");

@@ -1,0 +1,674 @@
+// p2_tc.cu -- pass 2 of the mixed-precision path on the 5th-generation tensor
+// cores (tcgen05), the same sum as p2_kernel<float, 2, TS>:
+//   F[mu][n] = sum_k Dr_mu[k] Bt[k][n],  dtmp = -sum_{mu,n} coef[mu][n] F[mu][n]
+// (ker_4pt_contraction, cuda_lattice.cu:277-484, restructured as in
+// contract_kernels.cuh).
+//
+// Per CTA (one per SM, persistent over tiles of 32 sites) and per phase
+// (tile, flavour f): the 128 x 160 product F = A . B^T, A = Dr with rows
+// (mu, site) = mu*32 + site and K = 288 = (p, q, re/im), B = Bt^T. Products
+// are FP32 in the 3xTF32 form A_hi B_hi + A_hi B_lo + A_lo B_hi (hi = the
+// TF32 rounding, lo = the TF32 rounding of the rest), accumulated in TMEM.
+//
+// Warp roles (15 warps):
+//   0      TMA producer of the FP32 input rows (S = x[1-f] rows q, Y = y[f]
+//          rows p: 3 KB per (flavour, ia, tile)) -- one thread
+//   1      TMA producer of the B chunks (16 k x 160 n, hi and lo, 20 KB) -- one thread
+//   2      TMEM allocation; tcgen05.mma issue and commits -- one thread
+//   3-10   D formation: per chunk of 16 k (8 (p, q)), warp w forms (p, q) =
+//          the chunk's w-th for its lane's site: O = Y conj(S) spin blocks
+//          -> D_mu -> hi/lo -> shared memory in the K-major no-swizzle
+//          core-matrix layout
+//   11-14  epilogue: one TMEM lane quadrant each (warp % 4 = mu); per phase,
+//          the F rows from TMEM dotted with the QED coefficients of the
+//          row's site, into a compensated FP64 sum
+// The tensor cores accumulate in FP32 with truncation, so the small hi.lo
+// and lo.hi products would lose most of their bits if added into the large
+// hi.hi sum: they go to their own accumulator, which the epilogue folds
+// into the main one (FP32, round-to-nearest) before the dot.
+// Pipelines (mbarriers; every wait bounded, kWaitLimit polls):
+//   rows -> D warps (S double buffer per phase, Y ring of 4 rows),
+//   D warps -> MMA (A ring of 3), B producer -> MMA (B ring of 4),
+//   MMA -> epilogue (2 main accumulators and 1 correction accumulator of
+//   160 TMEM columns each).
+//
+// Inputs are the FP32 tile copies pass 1 writes while it converts each
+// block (x32/y32: [f][ia][tile][6][32][4] floats, a site's 24 components as
+// six 16-byte groups, 32 sites per tile), so pass 2 reads half the bytes of
+// the FP64 blocks and converts nothing.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <type_traits>
+
+#include "contract_kernels.cuh"
+#include "hlbl_gb300.h"
+#include "hlbl_internal.h"
+#include "p2_tc.h"
+
+namespace hg {
+namespace tc {
+
+constexpr int kSites = 32;                 // sites per tile
+constexpr int kM = 128;                    // MMA rows: (mu, site)
+constexpr int kKc = 16;                    // K per chunk
+constexpr int kChunks = kBtK / kKc;        // 18
+constexpr int kAStages = 3, kBStages = 4, kYSlots = 4, kAcc = 2;
+constexpr uint32_t kCorrCol = kAcc * kBtN;  // the correction accumulator's first column
+constexpr int kAPart = kM * kKc;           // floats per A part (hi or lo)
+constexpr int kBPart = kBtN * kKc;         // floats per B part
+constexpr int kWarpRows = 0, kWarpB = 1, kWarpMma = 2, kWarpD0 = 3, kDWarps = 8;
+constexpr int kWarpE0 = kWarpD0 + kDWarps, kEWarps = 4;
+constexpr int kThreads = 32 * (kWarpE0 + kEWarps);
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kRowBytes = kRowF32 * 4;  // 3072
+
+// instruction descriptor, kind::tf32: D F32, A and B TF32, both K-major,
+// N = 160, M = 128
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kBtN >> 3) << 17) |
+                            ((uint32_t)(kM >> 4) << 24);
+
+struct __align__(1024) Smem {
+  float S[2][12][kRowF32];
+  float Y[kYSlots][kRowF32];
+  float A[kAStages][2][kAPart];
+  float B[kBStages][2][kBPart];
+  uint64_t s_full[2], s_empty[2], y_full[kYSlots], y_empty[kYSlots];
+  uint64_t a_full[kAStages], a_empty[kAStages], b_full[kBStages], b_empty[kBStages];
+  uint64_t acc_full[kAcc], acc_empty[kAcc], corr_empty, mma_done;
+  uint32_t taddr;
+  int fail;
+  double red[kEWarps][2][2];
+};
+
+// ---- tcgen05 / TMA helpers ---------------------------------------------------
+// shared-memory matrix descriptor, no swizzle: start, leading byte offset
+// (between core matrices along K), stride byte offset (between 8-row groups)
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t addr, float v[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(addr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tmem_st16(uint32_t addr, const float v[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(addr),
+      "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+      "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+      "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+      "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// A wait that gives up when the CTA has failed or after kWaitLimit polls
+// (then it marks the CTA failed). Returns false on give-up.
+__device__ __forceinline__ bool wait_or_fail(uint64_t* bar, uint32_t parity, volatile int* fail) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 63) == 63 && *fail) return false;
+  }
+  *fail = 1;
+  return false;
+}
+
+// ---- the QED-weighted dot of one row (mu = MU, fixed) ------------------------------
+// The row's contribution is sum_n coef[MU][n] F[n] with n = (j, nu, lam),
+// coef[MU][(k, nu, lam)] = E1(k, MU, nu, lam) + E2(k, nu, MU, lam) - E3(k, lam, nu, MU)
+// (k < 6) and coef[MU][(6 + tau, nu, lam)] = sum_k c_k(tau) E3(k, lam, nu, MU)
+// with c_k(tau) = [sigma_k = tau] zh_rho_k - [rho_k = tau] zh_sigma_k, where
+// Ee(k, a, b, c) = kerv[k][a][b][c] of the stand-in tensor at the argument
+// pair e: (xm, ym), (ym, xm), (xm, x - y) (hlbl_qed_entry: six terms w_0..w_5,
+// each a Kronecker structure times coordinates). For fixed k the columns of
+// F form a 4 x 4 matrix G[nu][lam], and each term's sum over (nu, lam)
+// reduces to rows G.v, columns u.G, forms u.G.v, the trace and the
+// antisymmetric part G[r][s] - G[s][r]; the sums below are those reductions.
+struct SiteQ {
+  float xm[4], ym[4], xmy[4], zh[4];
+  float w[3][HLBL_QED_NW];
+};
+
+__device__ __forceinline__ float row_dot(const float* G, int i, const float* v) {
+  return fmaf(G[4 * i + 3], v[3], fmaf(G[4 * i + 2], v[2], fmaf(G[4 * i + 1], v[1], G[4 * i] * v[0])));
+}
+__device__ __forceinline__ float col_dot(const float* G, int i, const float* u) {
+  return fmaf(u[3], G[12 + i], fmaf(u[2], G[8 + i], fmaf(u[1], G[4 + i], u[0] * G[i])));
+}
+
+// sum_{nu,lam} E3(k, lam, nu, MU) G[nu][lam]; gx = G.xm, gz = G.xmy (rows),
+// zg = xmy.G (columns), xGx = xm.G.xm, tr = trace(G)
+template <int MU, int K>
+__device__ __forceinline__ float d3(const float* G, const SiteQ& q, const float* gx, const float* gz,
+                                    const float* zg, float xGx, float tr) {
+  constexpr int r = comb_rho(K), s = comb_sigma(K);
+  const float* x = q.xm;
+  const float* y = q.xmy;
+  const float* w = q.w[2];
+  float const anti = G[4 * r + s] - G[4 * s + r];
+  float v = -w[0] * x[MU] * anti;
+  v = fmaf(w[3] * (x[r] * y[s] - x[s] * y[r]) * (x[MU] + y[MU]), tr, v);
+  v = fmaf(w[4] * y[MU], x[r] * zg[s] - x[s] * zg[r], v);
+  if constexpr (MU == s) v += w[1] * zg[r] + w[2] * (gx[r] - gz[r]) + w[5] * y[r] * xGx;
+  if constexpr (MU == r) v -= w[1] * zg[s] + w[2] * (gx[s] - gz[s]) + w[5] * y[s] * xGx;
+  return v;
+}
+
+// j = K < 6: E1 + E2 - E3 against G = F[(K, ., .)]
+template <int MU, int K>
+__device__ __forceinline__ float dot_k(const float* G, const SiteQ& q) {
+  constexpr int r = comb_rho(K), s = comb_sigma(K);
+  const float* xm = q.xm;
+  const float* ym = q.ym;
+  const float* xmy = q.xmy;
+  float gx[4], gy[4], gz[4], zg[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    gx[i] = row_dot(G, i, xm);
+    gy[i] = row_dot(G, i, ym);
+  }
+  gz[r] = row_dot(G, r, xmy); gz[s] = row_dot(G, s, xmy);
+  zg[r] = col_dot(G, r, xmy); zg[s] = col_dot(G, s, xmy);
+  float const ygr = col_dot(G, r, ym), ygs = col_dot(G, s, ym);  // ym.G
+  float const xgr = col_dot(G, r, xm), xgs = col_dot(G, s, xm);  // xm.G
+  float const yGy = fmaf(ym[3], gy[3], fmaf(ym[2], gy[2], fmaf(ym[1], gy[1], ym[0] * gy[0])));
+  float const xGx = fmaf(xm[3], gx[3], fmaf(xm[2], gx[2], fmaf(xm[1], gx[1], xm[0] * gx[0])));
+  float const tr = G[0] + G[5] + G[10] + G[15];
+  float const anti = G[4 * r + s] - G[4 * s + r];
+  const float* w1 = q.w[0];
+  const float* w2 = q.w[1];
+  // E1: (a, b, c) = (MU, nu, lam) at (xm, ym)
+  float v = w1[2] * (xm[MU] - ym[MU]) * anti;
+  v = fmaf(w1[3] * (xm[r] * ym[s] - xm[s] * ym[r]), gx[MU] + gy[MU], v);
+  v = fmaf(w1[5] * xm[MU], ym[r] * xgs - ym[s] * xgr, v);
+  if constexpr (MU == r) v += w1[0] * gx[s] + w1[1] * ygs - w1[4] * xm[s] * yGy;
+  if constexpr (MU == s) v += -w1[0] * gx[r] - w1[1] * ygr + w1[4] * xm[r] * yGy;
+  // E2: (a, b, c) = (nu, MU, lam) at (ym, xm)
+  v = fmaf(w2[1] * xm[MU], anti, v);
+  v = fmaf(w2[3] * (ym[r] * xm[s] - ym[s] * xm[r]), gy[MU] + gx[MU], v);
+  v = fmaf(w2[4] * xm[MU], ym[r] * gx[s] - ym[s] * gx[r], v);
+  v = fmaf(w2[5] * ym[MU], xm[r] * ygs - xm[s] * ygr, v);
+  if constexpr (MU == s) v += w2[0] * gy[r] - w2[2] * (ygr - xgr);
+  if constexpr (MU == r) v += -w2[0] * gy[s] + w2[2] * (ygs - xgs);
+  // - E3: (a, b, c) = (lam, nu, MU) at (xm, x - y)
+  return v - d3<MU, K>(G, q, gx, gz, zg, xGx, tr);
+}
+
+// j = 6 + TAU: sum_k c_k(TAU) E3(k, lam, nu, MU) against G = F[(6 + TAU, ., .)]
+template <int MU, int TAU>
+__device__ __forceinline__ float dot_zh(const float* G, const SiteQ& q) {
+  float gx[4], gz[4], zg[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    gx[i] = row_dot(G, i, q.xm);
+    gz[i] = row_dot(G, i, q.xmy);
+    zg[i] = col_dot(G, i, q.xmy);
+  }
+  const float* xm = q.xm;
+  float const xGx = fmaf(xm[3], gx[3], fmaf(xm[2], gx[2], fmaf(xm[1], gx[1], xm[0] * gx[0])));
+  float const tr = G[0] + G[5] + G[10] + G[15];
+  float v = 0.f;
+  auto term = [&](auto kc) {
+    constexpr int k = decltype(kc)::value;
+    constexpr int r = comb_rho(k), g = comb_sigma(k);
+    if constexpr (g == TAU || r == TAU) {
+      float const e = d3<MU, k>(G, q, gx, gz, zg, xGx, tr);
+      if constexpr (g == TAU) v = fmaf(q.zh[r], e, v);
+      if constexpr (r == TAU) v = fmaf(-q.zh[g], e, v);
+    }
+  };
+  term(std::integral_constant<int, 0>{});
+  term(std::integral_constant<int, 1>{});
+  term(std::integral_constant<int, 2>{});
+  term(std::integral_constant<int, 3>{});
+  term(std::integral_constant<int, 4>{});
+  term(std::integral_constant<int, 5>{});
+  return v;
+}
+
+// One phase's row: sum_n coef[MU][n] F[n], F at column c of this warp's lane
+// quadrant (16 columns = one 4 x 4 matrix per j).
+template <int MU>
+__device__ __noinline__ float epilogue_row(uint32_t lane_addr, uint32_t c, const SiteQ& q) {
+  float f[16], a = 0.f;
+#define HG_TC_K(J)                      \
+  tmem_ld16(lane_addr + c + 16 * J, f); \
+  tmem_wait_ld();                       \
+  a += dot_k<MU, J>(f, q);
+#define HG_TC_T(J)                      \
+  tmem_ld16(lane_addr + c + 16 * J, f); \
+  tmem_wait_ld();                       \
+  a += dot_zh<MU, J - 6>(f, q);
+  HG_TC_K(0) HG_TC_K(1) HG_TC_K(2) HG_TC_K(3) HG_TC_K(4) HG_TC_K(5)
+  HG_TC_T(6) HG_TC_T(7) HG_TC_T(8) HG_TC_T(9)
+#undef HG_TC_K
+#undef HG_TC_T
+  return a;
+}
+
+// ---- the kernel ------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads, 1)
+p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu,
+            double* __restrict__ partials, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+  volatile int* fail = &sm.fail;
+  int const t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  int const pi = blockIdx.y;
+  long long const ntiles = (geo.V + kSites - 1) / kSites;
+  long long const my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  int const nph = (int)(2 * my_tiles);
+  const float* __restrict__ x32 = tb.x32[pi];
+  const float* __restrict__ y32 = tb.y32;
+  auto row_ptr = [&](const float* base, int f, int ia, long long tile) {
+    return base + ((size_t)(f * 12 + ia) * ntiles + tile) * kRowF32;
+  };
+
+  if (t == 0) {
+    for (int i = 0; i < 2; ++i) { mbar_init(&sm.s_full[i], 1); mbar_init(&sm.s_empty[i], kDWarps); }
+    for (int i = 0; i < kYSlots; ++i) { mbar_init(&sm.y_full[i], 1); mbar_init(&sm.y_empty[i], kDWarps); }
+    for (int i = 0; i < kAStages; ++i) { mbar_init(&sm.a_full[i], kDWarps); mbar_init(&sm.a_empty[i], 1); }
+    for (int i = 0; i < kBStages; ++i) { mbar_init(&sm.b_full[i], 1); mbar_init(&sm.b_empty[i], 1); }
+    for (int i = 0; i < kAcc; ++i) { mbar_init(&sm.acc_full[i], 1); mbar_init(&sm.acc_empty[i], kEWarps); }
+    mbar_init(&sm.corr_empty, kEWarps);
+    mbar_init(&sm.mma_done, 1);
+    fence_mbar_init();
+    sm.fail = 0;
+  }
+  if (warp == kWarpMma) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.taddr)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  uint32_t const tmem = sm.taddr;
+
+  // issue tracking for the teardown after a failure
+  int rows_issued_s = -1, rows_issued_y = -1;  // last phase / row-use index issued
+  int b_issued = -1;
+  bool mma_any = false;
+
+  if (warp == kWarpRows) {
+    // ---- input rows ---------------------------------------------------------
+    if (lane == 0 && nph > 0) {
+      auto issue_S = [&](int P) -> bool {
+        int const buf = P & 1, f = P & 1;
+        long long const tile = blockIdx.x + (long long)(P >> 1) * gridDim.x;
+        if (!wait_or_fail(&sm.s_empty[buf], (uint32_t)(((P >> 1) & 1) ^ 1), fail)) return false;
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&sm.s_full[buf], 12 * kRowBytes);
+        for (int q = 0; q < 12; ++q) bulk_g2s(sm.S[buf][q], row_ptr(x32, 1 - f, q, tile), kRowBytes, &sm.s_full[buf]);
+        rows_issued_s = P;
+        return true;
+      };
+      bool ok = issue_S(0);
+      for (int P = 0; ok && P < nph; ++P) {
+        int const f = P & 1;
+        long long const tile = blockIdx.x + (long long)(P >> 1) * gridDim.x;
+        for (int p = 0; ok && p < 12; ++p) {
+          int const uy = P * 12 + p, slot = p % kYSlots;
+          if (!wait_or_fail(&sm.y_empty[slot], (uint32_t)(((uy / kYSlots) & 1) ^ 1), fail)) { ok = false; break; }
+          fence_proxy_async_smem();
+          mbar_arrive_expect_tx(&sm.y_full[slot], kRowBytes);
+          bulk_g2s(sm.Y[slot], row_ptr(y32, f, p, tile), kRowBytes, &sm.y_full[slot]);
+          rows_issued_y = uy;
+          if (p == 1 && P + 1 < nph) ok = issue_S(P + 1);
+        }
+      }
+    }
+  } else if (warp == kWarpB) {
+    // ---- B chunks -------------------------------------------------------------
+    if (lane == 0) {
+      int bc = 0;
+      bool ok = true;
+      for (int P = 0; ok && P < nph; ++P) {
+        const float* src = btu + ((size_t)pi * 2 + (P & 1)) * kChunks * 2 * kBPart;
+        for (int c = 0; c < kChunks; ++c, ++bc) {
+          int const st = bc % kBStages;
+          if (!wait_or_fail(&sm.b_empty[st], (uint32_t)(((bc / kBStages) & 1) ^ 1), fail)) { ok = false; break; }
+          fence_proxy_async_smem();
+          mbar_arrive_expect_tx(&sm.b_full[st], 2 * kBPart * 4);
+          bulk_g2s(sm.B[st][0], src + (size_t)c * 2 * kBPart, 2 * kBPart * 4, &sm.b_full[st]);
+          b_issued = bc;
+        }
+      }
+    }
+  } else if (warp == kWarpMma) {
+    // ---- MMA issue ----------------------------------------------------------------
+    if (lane == 0) {
+      int ac = 0, bc = 0;
+      bool ok = true;
+      for (int P = 0; ok && P < nph; ++P) {
+        int const buf = P % kAcc;
+        if (!wait_or_fail(&sm.acc_empty[buf], (uint32_t)(((P / kAcc) & 1) ^ 1), fail) ||
+            !wait_or_fail(&sm.corr_empty, (uint32_t)((P & 1) ^ 1), fail))
+          break;
+        tc_fence_after();
+        uint32_t const d = tmem + (uint32_t)(buf * kBtN), dc = tmem + kCorrCol;
+        for (int c = 0; c < kChunks; ++c, ++ac, ++bc) {
+          int const as = ac % kAStages, bs = bc % kBStages;
+          if (!wait_or_fail(&sm.a_full[as], (uint32_t)((ac / kAStages) & 1), fail) ||
+              !wait_or_fail(&sm.b_full[bs], (uint32_t)((bc / kBStages) & 1), fail)) { ok = false; break; }
+          tc_fence_after();
+          uint32_t const a0 = smem_u32(sm.A[as][0]), b0 = smem_u32(sm.B[bs][0]);
+#pragma unroll
+          for (int ks = 0; ks < 2; ++ks) {
+            // hi.hi into the main accumulator, hi.lo and lo.hi into the
+            // correction accumulator; parts are kAPart*4 / kBPart*4 bytes
+            // apart, k-steps 2 core columns (2*16*128 / 2*20*128 bytes) apart
+            uint32_t const ak = a0 + ks * 2 * (kM / 8) * 128, bk = b0 + ks * 2 * (kBtN / 8) * 128;
+            uint64_t const ahi = sdesc(ak, (kM / 8) * 128, 128), alo = sdesc(ak + kAPart * 4, (kM / 8) * 128, 128);
+            uint64_t const bhi = sdesc(bk, (kBtN / 8) * 128, 128), blo = sdesc(bk + kBPart * 4, (kBtN / 8) * 128, 128);
+            uint32_t const acc = (c | ks) ? 1u : 0u;
+            mma_tf32(d, ahi, bhi, acc);
+            mma_tf32(dc, ahi, blo, acc);
+            mma_tf32(dc, alo, bhi, 1u);
+          }
+          mma_any = true;
+          mma_commit(&sm.a_empty[as]);
+          mma_commit(&sm.b_empty[bs]);
+        }
+        if (!ok) break;
+        mma_commit(&sm.acc_full[buf]);
+      }
+    }
+  } else if (warp < kWarpE0) {
+    // ---- D formation ----------------------------------------------------------------
+    int const j = warp - kWarpD0;  // the chunk's (p, q) this warp forms
+    int const s = lane;
+    int ac = 0;
+    bool ok = true;
+    for (int P = 0; ok && P < nph; ++P) {
+      long long const tile = blockIdx.x + (long long)(P >> 1) * gridDim.x;
+      int const nvalid = (int)min((long long)kSites, geo.V - tile * kSites);
+      if (!wait_or_fail(&sm.s_full[P & 1], (uint32_t)((P >> 1) & 1), fail)) break;
+      const float* Sb = sm.S[P & 1][0];
+      int pw = -1;  // Y rows of this phase waited for
+      for (int c = 0; c < kChunks; ++c, ++ac) {
+        int const pmax = (8 * c + 7) / 12;
+        while (ok && pw < pmax) {
+          ++pw;
+          ok = wait_or_fail(&sm.y_full[pw % kYSlots], (uint32_t)(((P * 12 + pw) / kYSlots) & 1), fail);
+        }
+        int const as = ac % kAStages;
+        if (!ok || !wait_or_fail(&sm.a_empty[as], (uint32_t)(((ac / kAStages) & 1) ^ 1), fail)) { ok = false; break; }
+        int const pq = 8 * c + j, p = pq / 12, q = pq % 12;
+        // k = 2j + {re, im}: core column j/2, elements 2(j%2), 2(j%2)+1 of the
+        // row (mu*32 + s)
+        float* Ahi = sm.A[as][0] + (j >> 1) * 16 * 32 + s * 4 + 2 * (j & 1);
+        float* Alo = sm.A[as][1] + (j >> 1) * 16 * 32 + s * 4 + 2 * (j & 1);
+        if (s < nvalid) {
+          const float* Yr = sm.Y[p % kYSlots] + s * 4;
+          const float* Sr = Sb + q * kRowF32 + s * 4;
+          float y[24], x[24];
+#pragma unroll
+          for (int c4 = 0; c4 < 6; ++c4) {
+            float4 const a = *reinterpret_cast<const float4*>(Yr + c4 * 128);
+            float4 const b = *reinterpret_cast<const float4*>(Sr + c4 * 128);
+            y[4 * c4] = a.x; y[4 * c4 + 1] = a.y; y[4 * c4 + 2] = a.z; y[4 * c4 + 3] = a.w;
+            x[4 * c4] = b.x; x[4 * c4 + 1] = b.y; x[4 * c4 + 2] = b.z; x[4 * c4 + 3] = b.w;
+          }
+          // O[s1][s2] = sum_c Y[s1][c] conj(S[s2][c]), s2 = s1^2 (a) and 3-s1 (b)
+          float oa[4][2], ob[4][2];
+#pragma unroll
+          for (int s1 = 0; s1 < 4; ++s1) {
+            float ar = 0, ai = 0, br = 0, bi = 0;
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) {
+              float const yr = y[2 * (3 * s1 + cc)], yi = y[2 * (3 * s1 + cc) + 1];
+              int const sa = 2 * (3 * (s1 ^ 2) + cc), sb = 2 * (3 * (3 - s1) + cc);
+              ar += yr * x[sa] + yi * x[sa + 1];  ai += yi * x[sa] - yr * x[sa + 1];
+              br += yr * x[sb] + yi * x[sb + 1];  bi += yi * x[sb] - yr * x[sb + 1];
+            }
+            oa[s1][0] = ar; oa[s1][1] = ai; ob[s1][0] = br; ob[s1][1] = bi;
+          }
+#pragma unroll
+          for (int mu = 0; mu < 4; ++mu) {
+            float dr = 0, di = 0;
+#pragma unroll
+            for (int s1 = 0; s1 < 4; ++s1) {
+              float const* o = (mu == 0 || mu == 3) ? oa[s1] : ob[s1];
+              float vr, vi;
+              mul_iph((6 - g5g_ph(mu, s1)) & 3, o[0], o[1], vr, vi);
+              dr += vr; di += vi;
+            }
+            float const hr = __uint_as_float(tf32_rna(dr)), hi_ = __uint_as_float(tf32_rna(di));
+            *reinterpret_cast<float2*>(Ahi + mu * 4 * 32) = make_float2(hr, hi_);
+            *reinterpret_cast<float2*>(Alo + mu * 4 * 32) =
+                make_float2(__uint_as_float(tf32_rna(dr - hr)), __uint_as_float(tf32_rna(di - hi_)));
+          }
+        } else {
+          float2 const z = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int mu = 0; mu < 4; ++mu) {
+            *reinterpret_cast<float2*>(Ahi + mu * 4 * 32) = z;
+            *reinterpret_cast<float2*>(Alo + mu * 4 * 32) = z;
+          }
+        }
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+          mbar_arrive(&sm.a_full[as]);
+          // Y rows whose last chunk this was
+          for (int pp = (8 * c) / 12; pp <= pmax; ++pp)
+            if ((12 * pp + 11) / 8 == c) mbar_arrive(&sm.y_empty[pp % kYSlots]);
+        }
+      }
+      if (!ok) break;
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.s_empty[P & 1]);
+    }
+  } else {
+    // ---- epilogue -----------------------------------------------------------------------
+    int const quad = warp & 3;  // the TMEM lanes this warp may access; mu = quad
+    int const s = lane;
+    uint32_t const lane_addr = tmem + ((uint32_t)(quad * 32) << 16);
+    const int gsx[4] = {tb.gsx[pi][0], tb.gsx[pi][1], tb.gsx[pi][2], tb.gsx[pi][3]};
+    const int yv[4] = {tb.yv[pi][0], tb.yv[pi][1], tb.yv[pi][2], tb.yv[pi][3]};
+    const double* __restrict__ wq = args.w + (size_t)pi * geo.V * 3 * HLBL_QED_NW;
+    double const xu = args.xunit;
+    SiteQ q;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) q.ym[r] = (float)(coord_map(mod_pos(yv[r], geo.global[r]), geo.global[r]) * xu);
+    Neu run0, run1;
+    for (int P = 0; P < nph; ++P) {
+      long long const tile = blockIdx.x + (long long)(P >> 1) * gridDim.x;
+      long long const v = tile * kSites + s;
+      bool const valid = v < geo.V;
+      if ((P & 1) == 0) {
+        // the row's site data, for both flavours of the tile
+        long long const vv = valid ? v : geo.V - 1;
+        int rel[4];
+        rel_coords(geo, gsx, vv, rel);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          q.xm[r] = (float)(coord_map(rel[r], geo.global[r]) * xu);
+          q.xmy[r] = (float)(coord_map_diff(rel[r], yv[r], geo.global[r]) * xu);
+          q.zh[r] = (float)coord_map_zerohalf(rel[r], geo.global[r]);
+        }
+#pragma unroll
+        for (int e = 0; e < 3; ++e)
+#pragma unroll
+          for (int k = 0; k < HLBL_QED_NW; ++k) q.w[e][k] = (float)wq[((size_t)vv * 3 + e) * HLBL_QED_NW + k];
+      }
+      int const buf = P % kAcc;
+      if (!wait_or_fail(&sm.acc_full[buf], (uint32_t)((P / kAcc) & 1), fail)) break;
+      tc_fence_after();
+      uint32_t const c0 = (uint32_t)(buf * kBtN);
+      // fold the corrections into the main accumulator, then free them
+#pragma unroll 1
+      for (int jj = 0; jj < 10; ++jj) {
+        float m[16], k[16];
+        tmem_ld16(lane_addr + c0 + 16 * jj, m);
+        tmem_ld16(lane_addr + kCorrCol + 16 * jj, k);
+        tmem_wait_ld();
+#pragma unroll
+        for (int i = 0; i < 16; ++i) m[i] += k[i];
+        tmem_st16(lane_addr + c0 + 16 * jj, m);
+      }
+      tmem_wait_st();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.corr_empty);
+      tc_fence_after();
+      float a;
+      switch (quad) {
+        case 0: a = epilogue_row<0>(lane_addr, c0, q); break;
+        case 1: a = epilogue_row<1>(lane_addr, c0, q); break;
+        case 2: a = epilogue_row<2>(lane_addr, c0, q); break;
+        default: a = epilogue_row<3>(lane_addr, c0, q); break;
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.acc_empty[buf]);
+      if (valid) {
+        if (P & 1) run1.add(-(double)a);
+        else run0.add(-(double)a);
+      }
+    }
+    if (!*fail) {
+      // fixed-order compensated reduction over the epilogue's 128 threads
+      Neu r0 = run0, r1 = run1;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        double const s0v = __shfl_down_sync(0xffffffffu, r0.s, o), c0v = __shfl_down_sync(0xffffffffu, r0.c, o);
+        double const s1v = __shfl_down_sync(0xffffffffu, r1.s, o), c1v = __shfl_down_sync(0xffffffffu, r1.c, o);
+        r0.add(s0v); r0.c += c0v;
+        r1.add(s1v); r1.c += c1v;
+      }
+      if (lane == 0) {
+        int const ew = warp - kWarpE0;
+        sm.red[ew][0][0] = r0.s; sm.red[ew][0][1] = r0.c;
+        sm.red[ew][1][0] = r1.s; sm.red[ew][1][1] = r1.c;
+      }
+    }
+  }
+
+  // ---- teardown ----------------------------------------------------------------------------
+  tc_fence_before();
+  __syncthreads();
+  if (*fail) {
+    // let nothing this CTA started outlive it (each wait bounded)
+    if (warp == kWarpRows && lane == 0) {
+      if (rows_issued_s >= 0) mbar_wait(&sm.s_full[rows_issued_s & 1], (uint32_t)((rows_issued_s >> 1) & 1));
+      for (int u = rows_issued_y - kYSlots + 1; u <= rows_issued_y; ++u)
+        if (u >= 0) mbar_wait(&sm.y_full[u % kYSlots], (uint32_t)((u / kYSlots) & 1));
+    }
+    if (warp == kWarpB && lane == 0)
+      for (int u = b_issued - kBStages + 1; u <= b_issued; ++u)
+        if (u >= 0) mbar_wait(&sm.b_full[u % kBStages], (uint32_t)((u / kBStages) & 1));
+    if (warp == kWarpMma && lane == 0 && mma_any) {
+      mma_commit(&sm.mma_done);
+      mbar_wait(&sm.mma_done, 0);
+    }
+    if (t == 0 && err) atomicExch(err, kErrWaitTimeout);
+  } else if (t == kWarpE0 * 32) {
+    for (int f = 0; f < 2; ++f) {
+      Neu acc;
+      for (int w = 0; w < kEWarps; ++w) { acc.add(sm.red[w][f][0]); acc.c += sm.red[w][f][1]; }
+      partials[((size_t)pi * gridDim.x + blockIdx.x) * 2 + f] = acc.get();
+    }
+  }
+  __syncthreads();
+  tc_fence_after();
+  if (warp == kWarpMma)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+}
+
+// B operand of the tensor-core pass 2, from the gamma-inserted pass-1 sums:
+// per (pair, flavour) and chunk of 16 k, the 160 x 16 block of Bt^T as TF32
+// hi and lo parts in the K-major core-matrix layout (core (kg, n/8) at
+// (kg*20 + n/8)*128 bytes, row n%8 at 16 bytes, k%4 at 4 bytes). The values
+// are bt_build_kernel's.
+__global__ void btu_build_kernel(const double* __restrict__ g, int nf, float* __restrict__ btu) {
+  int const fl = blockIdx.y, pi = blockIdx.z;
+  int const i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kBtK * kBtN || fl >= nf) return;
+  const double* g_dzu = g + ((size_t)pi * nf + fl) * kGLen;
+  const double* g_dzsu = g_dzu + kGDzuLen;
+  int const k = i / kBtN, n = i % kBtN;
+  int const e = k & 1, pq = k >> 1, p = pq / 12, q = pq % 12;
+  int const lam = n & 3, nu = (n >> 2) & 3, j = n >> 4;
+  int const sq = q / 3, cq = q % 3;
+  int sq2 = 0;
+#pragma unroll
+  for (int s = 0; s < 4; ++s)
+    if (gg5_src(lam, s) == sq) sq2 = s;
+  int const ph = gg5_ph(lam, sq2);
+  const double* v = j < 6 ? g_dzu + ((((j * 4 + nu) * 12) + (3 * sq2 + cq)) * 12 + p) * 2
+                          : g_dzsu + (((((j - 6) * 4 + nu) * 12) + (3 * sq2 + cq)) * 12 + p) * 2;
+  double re, im;
+  mul_iph(ph, v[0], v[1], re, im);
+  double const x = e == 0 ? re : -im;
+  float const hi = __uint_as_float(tf32_rna((float)x));
+  float const lo = __uint_as_float(tf32_rna((float)(x - (double)hi)));
+  int const c = k / kKc, kk = k % kKc;
+  size_t const base = (((size_t)pi * 2 + fl) * kChunks + c) * 2 * kBPart;
+  int const off = ((kk >> 2) * (kBtN / 8) + (n >> 3)) * 32 + (n & 7) * 4 + (kk & 3);
+  btu[base + off] = hi;
+  btu[base + kBPart + off] = lo;
+}
+
+}  // namespace tc
+
+size_t tc_smem_bytes() { return sizeof(tc::Smem); }
+int tc_threads() { return tc::kThreads; }
+size_t tc_btu_floats_per_pair() { return (size_t)2 * tc::kChunks * 2 * tc::kBPart; }
+
+int tc_init(int nsm, int& grid) {
+  cudaError_t e = cudaFuncSetAttribute(tc::p2tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)sizeof(tc::Smem));
+  if (e != cudaSuccess) return cuda_fail(e, "p2tc smem attribute");
+  int nb = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tc::p2tc_kernel, tc::kThreads, sizeof(tc::Smem));
+  if (e != cudaSuccess) return cuda_fail(e, "p2tc occupancy");
+  if (nb < 1) return fail(HLBL_ECUDA, "p2tc kernel cannot be resident (smem %zu)", sizeof(tc::Smem));
+  // one CTA per SM: each allocates all 512 TMEM columns
+  grid = nsm;
+  return HLBL_OK;
+}
+
+void tc_launch_btu(const double* d_g, int npairs, float* d_btu, cudaStream_t st) {
+  dim3 const gb((kBtK * kBtN + 255) / 256, 2, npairs);
+  tc::btu_build_kernel<<<gb, 256, 0, st>>>(d_g, 2, d_btu);
+}
+
+void tc_launch_p2(int grid, int npairs, cudaStream_t st, const TcBatch& tb, const Geometry& geo,
+                  const P2Args& a, const float* d_btu, double* partials, int* err) {
+  tc::p2tc_kernel<<<dim3(grid, npairs), tc::kThreads, sizeof(tc::Smem), st>>>(tb, geo, a, d_btu, partials, err);
+}
+
+long long tc_tiles(long long V) { return (V + tc::kSites - 1) / tc::kSites; }
+
+}  // namespace hg

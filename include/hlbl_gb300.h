@@ -109,13 +109,21 @@ int hlbl_ctx_reserve(hlbl_ctx* ctx, int max_pairs);
 int hlbl_stage_async(hlbl_ctx* ctx, void* d_dst, const void* h_src, size_t bytes,
                      int after_compute);
 
-/* Autotuner: times one batch (FP32 products) under each FP32 tile variant
- * of pass 1 and pass 2 and each batch group (1, 2, 4, 8, 16 pairs per
- * launch) and keeps the fastest in the context. Writes the sums of the last
- * trial to d_out. Blocking. */
+/* Autotuner: times one batch (FP32 products) under each FP32 variant of
+ * pass 1 (best_p1: 0 = tiles of 8 sites, 1 = 4) and pass 2 (best_p2:
+ * 0 = CUDA cores, tiles of 4 sites; 1 = CUDA cores, 2 sites; 2 = tensor
+ * cores) and each batch group (1, 2, 4, 8, 16 pairs per launch) and keeps
+ * the fastest in the context. Writes the sums of the last trial to d_out.
+ * Blocking. No counterpart in the reference. */
 int hlbl_autotune(hlbl_ctx* ctx, const double* d_fwd_y, int n, const double* const* d_fwd_src,
                   const int* gsx, const int* yv, double xunit, double* d_out, int* best_p1,
                   int* best_p2, int* best_group, double* best_ms);
+
+/* FP32 two-flavour pass 2 on the tensor cores (on = 1, the default:
+ * tcgen05 MMAs with 3xTF32 products, FP32 tile copies of the blocks written
+ * by pass 1) or on the CUDA cores (on = 0). No counterpart in the
+ * reference. */
+int hlbl_ctx_set_tensor_cores(hlbl_ctx* ctx, int on);
 
 /* One CUDA graph per window: every asynchronous call made on the context
  * between hlbl_graph_begin and hlbl_graph_end (typically one

@@ -1,0 +1,69 @@
+"""The tensor-core pass 2 (tcgen05, 3xTF32 products) against the oracle and
+against the CUDA-core FP32 pass 2, through the C ABI: tail tiles (volumes
+that are not a multiple of the 32-site tile), tiny lattices, batches, and
+repeatability. Needs a GPU.
+
+Tolerance: 1e-4 relative per pair, the pair's two flavour sums as one
+vector (support.pair_rel_err), as for every FP32-product path."""
+import numpy as np
+import pytest
+
+import support as S
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+TOL32 = 1e-4
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+@pytest.mark.parametrize("lat", [(1, 1, 1, 1), (2, 2, 2, 2), (3, 5, 1, 7), (7, 3, 3, 3), (8, 4, 4, 4),
+                                 (16, 8, 8, 8)])
+def test_tensor_core_pass2_matches_oracle(lat):
+    import hlbl_gb300 as hg
+
+    src, y = S.gaussian_block(lat, 41), S.gaussian_block(lat, 42)
+    gsx = tuple(min(1, L - 1) for L in lat)
+    yv, xu = (1, -1, 1, 0), hg.xunit(105.658, 0.1)
+    orc = S.oracle_kernel_sum(src, y, gsx, yv, xu, lat)
+    with hg.Contractor(lat) as c:
+        d_src, d_y = dev(src), dev(y)
+        c.set_tensor_cores(True)
+        tc = c.kernel_sum(d_src, d_y, gsx, yv, xu, hg.FP32)
+        tc2 = c.kernel_sum(d_src, d_y, gsx, yv, xu, hg.FP32)
+        c.set_tensor_cores(False)
+        cc = c.kernel_sum(d_src, d_y, gsx, yv, xu, hg.FP32)
+    assert tc == tc2  # fixed-order reductions
+    assert S.pair_rel_err(tc, orc) <= TOL32, (tc, orc)
+    assert S.pair_rel_err(cc, orc) <= TOL32, (cc, orc)
+
+
+def test_tensor_core_batched_equals_per_pair():
+    """Five partners of one new block in one launch against one launch per
+    pair: the CTA partition of the sites differs, and with it the rounding of
+    pass 1's FP32 tile sums (flushed to FP64 every 32 sites of a CTA), so
+    the two agree to FP32 accuracy (1e-5 at the pair's scale); each is
+    within 1e-4 of the oracle."""
+    import hlbl_gb300 as hg
+
+    lat = (6, 4, 4, 4)
+    xu = hg.xunit(105.658, 0.1)
+    y = S.gaussian_block(lat, 7)
+    srcs = [S.gaussian_block(lat, 100 + i) for i in range(5)]
+    gsxs = [(i % 6, (i + 1) % 4, (2 * i) % 4, 3 - i % 4) for i in range(5)]
+    yvs = [(1, 0, -1, 1), (0, 1, 1, -1), (2, -1, 0, 0), (-1, -1, 1, 1), (1, 2, 0, -2)]
+    with hg.Contractor(lat) as c:
+        c.set_tensor_cores(True)
+        d_y = dev(y)
+        d_srcs = [dev(s) for s in srcs]
+        out = torch.zeros((5, 2), dtype=torch.float64, device="cuda")
+        c.kernel_sums_batched(d_y, d_srcs, gsxs, yvs, xu, out, hg.FP32)
+        c.check()
+        got = out.cpu().numpy()
+        for i in range(5):
+            one = c.kernel_sum(d_srcs[i], d_y, gsxs[i], yvs[i], xu, hg.FP32)
+            assert S.pair_rel_err(got[i], one) <= 1e-5
+            orc = S.oracle_kernel_sum(srcs[i], y, gsxs[i], yvs[i], xu, lat)
+            assert S.pair_rel_err(got[i], orc) <= TOL32
