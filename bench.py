@@ -98,6 +98,30 @@ def load_traffic():
         return None
 
 
+def measure_tf32_peak(torch):
+    """cuBLAS TF32 GEMM throughput (8192^3, FP32 in/out with TF32 math), best of 10."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    try:
+        n = 8192
+        a = torch.randn(n, n, device="cuda")
+        b = torch.randn(n, n, device="cuda")
+        for _ in range(3):
+            a @ b
+        best = 1e30
+        for _ in range(10):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            a @ b
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        del a, b
+        return 2 * n ** 3 / (best * 1e-3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle samples while the timed region runs."""
 
@@ -270,34 +294,28 @@ def main():
             ms = float(t.item())
         return n, ms
 
-    # ---- the learned QED weight, trained on this GPU before any timing -----
-    from hlbl_gb300.surrogate import Surrogate
+    def graph_timed(prec):
+        """Record the timed sources' batched calls as one CUDA graph and time
+        one replay (all K steps)."""
+        c.graph_begin()
+        run_batched(timed, prec, res)
+        graph = c.graph_end()
+        clocks = ClockSampler(local_rank)
+        n, ms = timeit(lambda: (graph.launch(stream), n_timed_pairs)[1])
+        graph.close()
+        return n, ms, clocks.stop()
 
-    sur = Surrogate(device=local_rank, seed=3)
-    t_train = time.perf_counter()
-    train_rep = sur.train(n_samples=args.train_samples, batch=8192, steps=args.train_steps,
-                          n_valid=1 << 18, bound=1e-5)
-    train_rep["wall_seconds"] = round(time.perf_counter() - t_train, 2)
-    train_rep["gain_max_err"] = train_rep["max_rel_err_base"] / max(train_rep["max_rel_err_net"], 1e-300)
-    train_rep["gain_rms_err"] = train_rep["rms_rel_err_base"] / max(train_rep["rms_rel_err_net"], 1e-300)
-
-    # ---- headline: batched, FP32 products, FP64 sums, learned weight, one
-    #      CUDA graph for the timed sources, autotuned tiles and grouping ----
-    c.set_qed(sur)
+    # ---- headline: batched per new source, FP32 products on the tensor
+    #      cores, FP64 sums, the exact QED weight (FP32 quadrature, FP64 near
+    #      the origin), one CUDA graph for the timed sources, autotuned -------
+    c.set_qed(None)
     c.reserve(16)
     y0, xs0, gs0, vs0 = step_args(warm[0] if warm else timed[0])
     tune = c.autotune(y0, xs0, gs0, vs0, xu, res[:len(xs0)])
     run_batched(warm, hg.FP32, res)
     stream.synchronize()
-    c.graph_begin()
-    run_batched(timed, hg.FP32, res)
-    graph = c.graph_end()
-    clocks = ClockSampler(local_rank)
-    n32, ms32 = timeit(lambda: (graph.launch(stream), n_timed_pairs)[1])
-    clk = clocks.stop()
-    res_sur = res.clone()
-    fallbacks = c.qed_fallbacks()
-    graph.close()
+    n32, ms32, clk = graph_timed(hg.FP32)
+    res_main = res.clone()
 
     # ---- the same without the graph, and per pair (unbatched) -------------
     res_b = torch.zeros_like(res)
@@ -306,11 +324,30 @@ def main():
     run_pairs(timed[:1], hg.FP32, res_p)
     npp, mspp = timeit(run_pairs, timed, hg.FP32, res_p)
 
-    # ---- batched FP32 products with the exact FP64 weight -------------------
+    # ---- the learned QED weight, trained on this GPU, in the same path ------
+    from hlbl_gb300.surrogate import Surrogate
+
+    sur = Surrogate(device=local_rank, seed=3)
+    t_train = time.perf_counter()
+    train_rep = sur.train(n_samples=args.train_samples, batch=8192, steps=args.train_steps,
+                          n_valid=1 << 18, bound=1e-4)
+    train_rep["wall_seconds"] = round(time.perf_counter() - t_train, 2)
+    train_rep["gain_max_err"] = train_rep["max_rel_err_base"] / max(train_rep["max_rel_err_net"], 1e-300)
+    train_rep["gain_rms_err"] = train_rep["rms_rel_err_base"] / max(train_rep["rms_rel_err_net"], 1e-300)
+    c.set_qed(sur)
+    run_batched(warm, hg.FP32, res)
+    c.set_qed(sur)  # fallback counter cleared: count the timed replay only
+    nsur, mssur, _ = graph_timed(hg.FP32)
+    res_sur = res.clone()
+    fallbacks = c.qed_fallbacks()
     c.set_qed(None)
+
+    # ---- FP32 products with the FP64 weight everywhere -----------------------
+    c.set_qed_fp32(False)
     res32x = torch.zeros_like(res)
     run_batched(timed[:1], hg.FP32, res32x)
     n32x, ms32x = timeit(run_batched, timed, hg.FP32, res32x)
+    c.set_qed_fp32(True)
 
     # ---- plain FP64, per pair, exact weight (the reference's path) on the
     #      first fp64-steps steps; the other timed pairs untimed (batched) so
@@ -335,18 +372,17 @@ def main():
         chain = ((a.sum(0) - a64.sum(0)).abs() / a64.sum(0).abs()).max().item()
         return per_pair, chain, per_flavour
 
-    rel, chain_rel, rel_fl = errs(res_sur)
+    rel, chain_rel, rel_fl = errs(res_main)
+    rel_sur, chain_sur, rel_sur_fl = errs(res_sur)
     rel32x, chain32x, rel32x_fl = errs(res32x)
     relp, _, _ = errs(res_p)
 
     # ---- per-kernel durations (CUDA events on the launching stream) --------
-    c.set_qed(sur)
     c.set_profiling(True)
     run_batched(timed[:1], hg.FP32, res_b)
     stream.synchronize()
     (p1ms, p1n), (p2ms, p2n) = c.kernel_times()
     c.set_profiling(False)
-    c.set_qed(None)
     c.set_profiling(True)
     run_pairs([(timed[0][0], timed[0][1][:1])], hg.FP64, res_b)
     stream.synchronize()
@@ -355,14 +391,12 @@ def main():
     n_prof = len(timed[0][1])
     g = tune["batch_group"]
     groups = [min(g, n_prof - i) for i in range(0, n_prof, g)]
-    # algorithmic bytes of one step's pass-2 launches: y once per launch plus
-    # each partner's block (both flavours, 4,608 B/site per block)
-    step_p2_bytes = sum((1 + gi) for gi in groups) * 2 * 12 * 24 * 8 * volume(LATTICE)
+    V = volume(LATTICE)
+    blk = 2 * 12 * 24 * 8 * V  # bytes of one FP64 block (4,608 B/site)
 
     # ---- end to end through the C ABI with host buffers: each step stages
     #      its new block from pinned host memory on the side stream (the
     #      next one while this one computes) and reads its sums back ---------
-    c.set_qed(sur)
     pinned = {}
     for p, _ in timed:
         site = schedule.mod_pos(p, LATTICE)
@@ -399,20 +433,37 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
 
-    # ---- peaks and roofline -----------------------------------------------
+    # ---- peaks and rooflines -------------------------------------------------
     peaks, peak_src = load_peaks()
     fp64_peak = measure_fma_peak(hg.FP64, local_rank)
     fp32_peak = measure_fma_peak(hg.FP32, local_rank)
-    V = volume(LATTICE)
+    tf32_peak = measure_tf32_peak(torch)
     p2_avg_ms = p2ms / max(1, p2n)
     p1_avg_ms = p1ms / max(1, p1n)
-    bytes_launch = step_p2_bytes / max(1, p2n)
-    achieved = step_p2_bytes / (p2ms * 1e-3) / 1e9
-    # pass-2 FLOPs per pair (both flavours, FMA = 2): GEMM 4x288x160, D
-    # formation 8 blocks x 144 x 3 complex MAC, coefficient dot
-    flop_pair = 2 * V * 2 * (4 * 288 * 160 + 8 * 144 * 3 * 4 + 640)
-    flop_p2 = flop_pair * n_prof / max(1, p2n)
     traffic = load_traffic()
+    # pass 1, per launch of g pairs: both FP64 blocks read (y once, each
+    # partner once) and their FP32 tile copies written (half the bytes)
+    p1_bytes = sum((1 + gi) for gi in groups) * blk * 1.5 / max(1, p1n)
+    p1_gbs = p1_bytes / (p1_avg_ms * 1e-3) / 1e9
+    # pass 2, per pair: the 128 x 160 x 288 product per 32 sites per flavour
+    # (FMA = 2 flops), algorithmic; the tensor cores issue 3x (3xTF32)
+    gemm_flop_pair = 2 * 2 * V * 4 * 288 * 160
+    p2_tflops = gemm_flop_pair * n_prof / max(1, p2n) / (p2_avg_ms * 1e-3) / 1e12
+    p2_bytes = sum((1 + gi) for gi in groups) * blk * 0.5 / max(1, p2n)  # FP32 tile copies read
+    rl_p1 = {"bound": "hbm", "kernel": f"pass 1, p1_kernel<float,2,{tune['p1_tile']}> (batched)",
+             "achieved": round(p1_gbs, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+             "frac": round(p1_gbs / peaks["hbm_gbs"], 5),
+             "traffic": (traffic or {}).get("p1_bytes_per_launch"),
+             "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+             "kernel_ms": round(p1_avg_ms, 3), "bytes_per_launch": p1_bytes}
+    rl_p2 = {"bound": "tensor", "kernel": f"pass 2, {tune['p2']} (batched)",
+             "achieved": round(p2_tflops, 2), "peak": round(tf32_peak, 1), "unit": "TFLOP/s",
+             "frac": round(p2_tflops / tf32_peak, 5),
+             "traffic": (traffic or {}).get("p2_bytes_per_launch"),
+             "peak_source": "measured here: cuBLAS TF32 GEMM 8192^3 (torch.matmul, allow_tf32)",
+             "issued_tf32_tflops": round(3 * p2_tflops, 2), "kernel_ms": round(p2_avg_ms, 3),
+             "hbm_gbs": round(p2_bytes / (p2_avg_ms * 1e-3) / 1e9, 2)}
+    dominant = rl_p1 if p1_avg_ms >= p2_avg_ms else rl_p2
 
     pairs_total = n32 * world
     value = pairs_total / (ms32 * 1e-3)
@@ -434,43 +485,40 @@ def main():
                                "(window 1 sources)",
                    "lattice": list(LATTICE), "pairs_timed": n32,
                    "path": "batched per source (autotuned), one CUDA graph for the timed sources; "
-                           "FP32 products, FP64 sums, learned QED weight",
-                   "qed_weight": "stand-in (KQED unavailable); headline: MLP surrogate with exact "
-                                 "FP64 fallback inside r0",
+                           "FP32 products (pass 2 on the tensor cores, 3xTF32), FP64 sums",
+                   "qed_weight": "stand-in (KQED unavailable), exact: FP32 quadrature, FP64 within "
+                                 "0.1/m_mu of the origin; the learned weight is the 'surrogate' line",
                    "l2": "inputs 3.06 GB per block, larger than L2; no flush"},
-        "fp64": {"value": round(n64 / (ms64 * 1e-3), 4), "unit": "pairs/s", "pairs_timed": n64,
-                 "path": "per pair, FP64 products, exact FP64 weight (the reference's algorithm)",
-                 "p2_kernel_ms": round(p2ms64 / max(1, p2n64), 3),
-                 "p1_kernel_ms": round(p1ms64 / max(1, p1n64), 3)},
-        "speedup_vs_fp64": round(value / (n64 / (ms64 * 1e-3)), 2),
         "max_rel_err_vs_fp64": rel,
         "max_rel_err_per_flavour_vs_fp64": rel_fl,
         "chain_total_rel_err_vs_fp64": chain_rel,
-        "batched_fp32_exact_qed": {"value": round(n32x / (ms32x * 1e-3), 4), "unit": "pairs/s",
-                                   "max_rel_err_vs_fp64": rel32x, "chain_total_rel_err_vs_fp64": chain32x,
-                                   "max_rel_err_per_flavour_vs_fp64": rel32x_fl},
-        "batched_surrogate_no_graph": {"value": round(nb_ / (msb * 1e-3), 4), "unit": "pairs/s"},
-        "per_pair_fp32_surrogate": {"value": round(npp / (mspp * 1e-3), 4), "unit": "pairs/s",
-                                    "max_rel_err_vs_fp64": relp},
+        "fp64": {"value": round(n64 / (ms64 * 1e-3), 4), "unit": "pairs/s", "pairs_timed": n64,
+                 "path": "per pair, FP64 products, exact FP64 weight (the reference's algorithm)",
+                 "p2_kernel_ms": round(p2ms64 / max(1, p2n64), 3),
+                 "p1_kernel_ms": round(p1ms64 / max(1, p1n64), 3),
+                 "fp64_fma_peak_tflops": round(fp64_peak, 3),
+                 "p2_fp64_tflops": round(gemm_flop_pair / (p2ms64 / max(1, p2n64) * 1e-3) / 1e12, 4)},
+        "speedup_vs_fp64": round(value / (n64 / (ms64 * 1e-3)), 2),
+        "surrogate": {"value": round(nsur / (mssur * 1e-3), 4), "unit": "pairs/s",
+                      "path": "the headline path with the MLP weight (exact FP64 outside its validated region)",
+                      "max_rel_err_vs_fp64": rel_sur, "chain_total_rel_err_vs_fp64": chain_sur,
+                      "max_rel_err_per_flavour_vs_fp64": rel_sur_fl,
+                      "train": train_rep, "fallback_rows_timed": fallbacks,
+                      "rows_timed": nsur * 3 * V},
+        "fp32_fp64_weight": {"value": round(n32x / (ms32x * 1e-3), 4), "unit": "pairs/s",
+                             "path": "batched, no graph, FP64 QED weight everywhere",
+                             "max_rel_err_vs_fp64": rel32x, "chain_total_rel_err_vs_fp64": chain32x,
+                             "max_rel_err_per_flavour_vs_fp64": rel32x_fl},
+        "batched_no_graph": {"value": round(nb_ / (msb * 1e-3), 4), "unit": "pairs/s"},
+        "per_pair": {"value": round(npp / (mspp * 1e-3), 4), "unit": "pairs/s", "max_rel_err_vs_fp64": relp},
         "autotune": tune,
-        "surrogate": {"train": train_rep, "fallback_rows_timed": fallbacks,
-                      "rows_timed": n32 * 3 * volume(LATTICE)},
         "e2e": {"value": round(pairs_total / e2e_s, 4), "unit": "pairs/s",
                 "h2d_bytes_per_step": int(h2d / max(1, len(timed))),
                 "d2h_bytes_per_step": int(d2h / max(1, len(timed)))},
-        "roofline": {"bound": "hbm", "kernel": f"pass 2, {tune['p2']} (batched)",
-                     "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": round(achieved / peaks["hbm_gbs"], 5),
-                     "traffic": (traffic or {}).get("bytes_per_launch"),
-                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                     "p2_kernel_ms": round(p2_avg_ms, 3), "p1_kernel_ms": round(p1_avg_ms, 3),
-                     "bytes_per_launch": bytes_launch},
-        "compute_roofline": {"bound": "fp32 fma", "achieved_tflops": round(flop_p2 / (p2_avg_ms * 1e-3) / 1e12, 3),
-                             "peak_tflops": round(fp32_peak, 2),
-                             "frac": round(flop_p2 / (p2_avg_ms * 1e-3) / 1e12 / fp32_peak, 4),
-                             "fp64_fma_peak_tflops": round(fp64_peak, 3),
-                             "fp64_p2_tflops": round(flop_p2 / (p2ms64 / max(1, p2n64) * 1e-3) / 1e12, 4),
-                             "peak_source": "measured here (FMA-chain kernel, hlbl_measure_fma_peak)"},
+        "roofline": dominant,
+        "rooflines": {"pass1": rl_p1, "pass2": rl_p2,
+                      "fp32_fma_peak_tflops": round(fp32_peak, 2),
+                      "fma_peak_source": "measured here (FMA-chain kernel, hlbl_measure_fma_peak)"},
         "clocks": clk,
         "gpu_launches": sum(7 * len([0 for _ in range(0, len(s[1]), tune["batch_group"])]) for s in timed),
     }

@@ -167,6 +167,11 @@ class Contractor:
                 "p2": ("cuda-core tile 4", "cuda-core tile 2", "tensor-core")[p2.value],
                 "batch_group": grp.value, "ms": ms.value}
 
+    def set_qed_fp32(self, on: bool = True, r64: float = 0.1) -> None:
+        """FP32 path's exact QED weight: FP32 quadrature outside min(|x|,|y|) < r64
+        (FP64 inside), or FP64 everywhere."""
+        check(lib.hlbl_ctx_set_qed_fp32(self._h, 1 if on else 0, float(r64)))
+
     def set_tensor_cores(self, on: bool) -> None:
         """FP32 two-flavour pass 2 on the tensor cores (default) or the CUDA cores."""
         check(lib.hlbl_ctx_set_tensor_cores(self._h, 1 if on else 0))

@@ -216,6 +216,9 @@ struct hlbl_ctx {
   long long w_cap = 0;        // sites d_w holds
   int batch_group = 0;        // pairs per batched launch (0: kMaxBatch)
   int qed_mode = HLBL_QED_EXACT;
+  // FP32 path, exact weight: FP32 quadrature outside qed_r64 (FP64 inside)
+  int qed_fp32 = 1;
+  double qed_r64 = 0.1;
   const hlbl_surrogate* sur = nullptr;
   double sur_r0 = 0.0;
   unsigned long long* d_fallback = nullptr;  // rows evaluated exactly inside r0
@@ -326,7 +329,7 @@ int run_pass1(hlbl_ctx* c, const Geometry& geo, const double* y, const PairBatch
 }
 
 // The QED weights of the batch's pairs into d_w ([pair][V][3][6]).
-int run_weights(hlbl_ctx* c, const Geometry& geo, const PairBatch& b, double xunit) {
+int run_weights(hlbl_ctx* c, const Geometry& geo, const PairBatch& b, double xunit, int precision) {
   long long const need = geo.V * b.n;
   if (need > c->w_cap) {
     if (c->capturing) return fail(HLBL_ESTATE, "QED weight buffer too small during graph capture");
@@ -346,7 +349,10 @@ int run_weights(hlbl_ctx* c, const Geometry& geo, const PairBatch& b, double xun
                                          c->nsm);
   long long const n = geo.V * 3;
   int const blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)c->nsm * 16 / b.n));
-  qed_weights_exact_kernel<<<dim3(blocks, b.n), 256, 0, c->stream>>>(geo, wa, c->d_w);
+  if (precision == HLBL_FP32 && c->qed_fp32)
+    qed_weights_fp32_kernel<<<dim3(blocks, b.n), 256, 0, c->stream>>>(geo, wa, c->qed_r64, c->d_w);
+  else
+    qed_weights_exact_kernel<<<dim3(blocks, b.n), 256, 0, c->stream>>>(geo, wa, c->d_w);
   return HLBL_OK;
 }
 
@@ -354,7 +360,7 @@ int run_weights(hlbl_ctx* c, const Geometry& geo, const PairBatch& b, double xun
 // b.p[i].out[0..nf) (added if add).
 int run_pass2(hlbl_ctx* c, const Geometry& geo, const double* y, const PairBatch& b, double xunit,
               int f0, int nf, int precision, int add) {
-  if (int rc = run_weights(c, geo, b, xunit)) return rc;
+  if (int rc = run_weights(c, geo, b, xunit, precision)) return rc;
   P2Args a{};
   a.xunit = xunit;
   a.f0 = f0;
@@ -570,6 +576,13 @@ int hlbl_kernel_sums_batched(hlbl_ctx* c, const double* y, int n, const double* 
     if (int rc = run_pass2(c, c->geo, y, b, xunit, 0, 2, precision, 0)) return rc;
   }
   return check_launch("hlbl_kernel_sums_batched launch");
+}
+
+int hlbl_ctx_set_qed_fp32(hlbl_ctx* c, int on, double r64) {
+  if (!c || !(r64 >= 0)) return fail(HLBL_EINVAL, "hlbl_ctx_set_qed_fp32: bad argument");
+  c->qed_fp32 = on ? 1 : 0;
+  c->qed_r64 = r64;
+  return HLBL_OK;
 }
 
 int hlbl_ctx_set_tensor_cores(hlbl_ctx* c, int on) {

@@ -491,6 +491,48 @@ static __global__ void qed_weights_exact_kernel(Geometry geo, WArgs args, double
   }
 }
 
+// The mixed-precision path's exact weight: the same 16-node quadrature in
+// FP32 where min(|x|, |y|) >= r64 (every quadrature term is positive, so
+// FP32 keeps ~1e-7 relative accuracy), in FP64 inside that radius (near the
+// origin) -- the FP64 QED evaluation is kept only there.
+static __global__ void qed_weights_fp32_kernel(Geometry geo, WArgs args, double r64, double* __restrict__ w) {
+  long long const n = geo.V * 3;
+  int const pi = blockIdx.y;
+  int const gsx[4] = {args.batch.p[pi].gsx[0], args.batch.p[pi].gsx[1], args.batch.p[pi].gsx[2], args.batch.p[pi].gsx[3]};
+  int const yv[4] = {args.batch.p[pi].yv[0], args.batch.p[pi].yv[1], args.batch.p[pi].yv[2], args.batch.p[pi].yv[3]};
+  w += (size_t)pi * n * HLBL_QED_NW;
+  float const l2 = (float)(args.qp.lambda * args.qp.lambda);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double a[4], b[4], X, c, Y, ww[HLBL_QED_NW];
+    qed_args(geo, gsx, yv, args.xunit, i / 3, (int)(i % 3), a, b);
+    hlbl_qed_invariants(a, b, &X, &c, &Y);
+    if (fmin(X, Y) < r64) {
+      hlbl_qed_weights(&args.qp, X, c, Y, ww);
+    } else {
+      float const xf = (float)X, yf = (float)Y, cf = (float)c;
+      float acc[HLBL_QED_NW];
+#pragma unroll
+      for (int j = 0; j < HLBL_QED_NW; ++j) acc[j] = 0.f;
+#pragma unroll 4
+      for (int q = 0; q < HLBL_QED_NQ; ++q) {
+        float const u = (float)args.qp.node[q], v = 1.f - u;
+        float r2 = u * u * xf * xf + v * v * yf * yf - 2.f * u * v * xf * yf * cf;
+        r2 = fmaxf(r2, 0.f);
+        float const g = (float)args.qp.weight[q] / (1.f + r2);
+        float const r = sqrtf(r2 + l2);
+        float const h[HLBL_QED_NW] = {1.f, u, v, u * v, u * u, v * v};
+#pragma unroll
+        for (int j = 0; j < HLBL_QED_NW; ++j) acc[j] += g * h[j] * expf(-(float)args.qp.mass[j] * r);
+      }
+#pragma unroll
+      for (int j = 0; j < HLBL_QED_NW; ++j) ww[j] = (double)acc[j];
+    }
+#pragma unroll
+    for (int j = 0; j < HLBL_QED_NW; ++j) w[i * HLBL_QED_NW + j] = ww[j];
+  }
+}
+
 struct P2Args {
   double xunit;
   int f0;                 // first flavour

@@ -22,15 +22,19 @@
 //   11-14  epilogue: one TMEM lane quadrant each (warp % 4 = mu); per phase,
 //          the F rows from TMEM dotted with the QED coefficients of the
 //          row's site, into a compensated FP64 sum
-// The tensor cores accumulate in FP32 with truncation, so the small hi.lo
-// and lo.hi products would lose most of their bits if added into the large
-// hi.hi sum: they go to their own accumulator, which the epilogue folds
-// into the main one (FP32, round-to-nearest) before the dot.
+// The tensor cores accumulate in FP32 with truncation (biased toward zero),
+// so the error grows with the number of MMAs added into one accumulator and
+// the small hi.lo and lo.hi products lose most of their bits if added into
+// the large hi.hi sum. Three accumulators of 160 TMEM columns: the
+// corrections go to their own, and the hi.hi sum of chunks 0-8 and of
+// chunks 9-17 to the two main buffers; the epilogue adds the second half
+// and the corrections into the first (FP32, round-to-nearest) before the
+// dot. The two main buffers swap roles every phase: the next phase's first
+// half only waits for that fold, its second half for the dot.
 // Pipelines (mbarriers; every wait bounded, kWaitLimit polls):
 //   rows -> D warps (S double buffer per phase, Y ring of 4 rows),
 //   D warps -> MMA (A ring of 3), B producer -> MMA (B ring of 4),
-//   MMA -> epilogue (2 main accumulators and 1 correction accumulator of
-//   160 TMEM columns each).
+//   MMA -> epilogue (acc_full), epilogue -> MMA (folded, dotted).
 //
 // Inputs are the FP32 tile copies pass 1 writes while it converts each
 // block (x32/y32: [f][ia][tile][6][32][4] floats, a site's 24 components as
@@ -53,8 +57,9 @@ constexpr int kSites = 32;                 // sites per tile
 constexpr int kM = 128;                    // MMA rows: (mu, site)
 constexpr int kKc = 16;                    // K per chunk
 constexpr int kChunks = kBtK / kKc;        // 18
-constexpr int kAStages = 3, kBStages = 4, kYSlots = 4, kAcc = 2;
-constexpr uint32_t kCorrCol = kAcc * kBtN;  // the correction accumulator's first column
+constexpr int kAStages = 3, kBStages = 4, kYSlots = 4;
+constexpr int kHalf = kChunks / 2;               // chunks per main-accumulator half
+constexpr uint32_t kCorrCol = 2 * kBtN;          // the correction accumulator's first column
 constexpr int kAPart = kM * kKc;           // floats per A part (hi or lo)
 constexpr int kBPart = kBtN * kKc;         // floats per B part
 constexpr int kWarpRows = 0, kWarpB = 1, kWarpMma = 2, kWarpD0 = 3, kDWarps = 8;
@@ -75,7 +80,7 @@ struct __align__(1024) Smem {
   float B[kBStages][2][kBPart];
   uint64_t s_full[2], s_empty[2], y_full[kYSlots], y_empty[kYSlots];
   uint64_t a_full[kAStages], a_empty[kAStages], b_full[kBStages], b_empty[kBStages];
-  uint64_t acc_full[kAcc], acc_empty[kAcc], corr_empty, mma_done;
+  uint64_t acc_full, folded, dotted, mma_done;
   uint32_t taddr;
   int fail;
   double red[kEWarps][2][2];
@@ -298,8 +303,9 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
     for (int i = 0; i < kYSlots; ++i) { mbar_init(&sm.y_full[i], 1); mbar_init(&sm.y_empty[i], kDWarps); }
     for (int i = 0; i < kAStages; ++i) { mbar_init(&sm.a_full[i], kDWarps); mbar_init(&sm.a_empty[i], 1); }
     for (int i = 0; i < kBStages; ++i) { mbar_init(&sm.b_full[i], 1); mbar_init(&sm.b_empty[i], 1); }
-    for (int i = 0; i < kAcc; ++i) { mbar_init(&sm.acc_full[i], 1); mbar_init(&sm.acc_empty[i], kEWarps); }
-    mbar_init(&sm.corr_empty, kEWarps);
+    mbar_init(&sm.acc_full, 1);
+    mbar_init(&sm.folded, kEWarps);
+    mbar_init(&sm.dotted, kEWarps);
     mbar_init(&sm.mma_done, 1);
     fence_mbar_init();
     sm.fail = 0;
@@ -370,13 +376,17 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
       int ac = 0, bc = 0;
       bool ok = true;
       for (int P = 0; ok && P < nph; ++P) {
-        int const buf = P % kAcc;
-        if (!wait_or_fail(&sm.acc_empty[buf], (uint32_t)(((P / kAcc) & 1) ^ 1), fail) ||
-            !wait_or_fail(&sm.corr_empty, (uint32_t)((P & 1) ^ 1), fail))
-          break;
+        // first half into main buffer P&1 (phase P-1's second half, free once
+        // folded), second half into buffer (P+1)&1 (free once dotted)
+        if (!wait_or_fail(&sm.folded, (uint32_t)((P & 1) ^ 1), fail)) break;
         tc_fence_after();
-        uint32_t const d = tmem + (uint32_t)(buf * kBtN), dc = tmem + kCorrCol;
+        uint32_t const dc = tmem + kCorrCol;
         for (int c = 0; c < kChunks; ++c, ++ac, ++bc) {
+          if (c == kHalf) {
+            if (!wait_or_fail(&sm.dotted, (uint32_t)((P & 1) ^ 1), fail)) { ok = false; break; }
+            tc_fence_after();
+          }
+          uint32_t const d = tmem + (uint32_t)(((c < kHalf ? P : P + 1) & 1) * kBtN);
           int const as = ac % kAStages, bs = bc % kBStages;
           if (!wait_or_fail(&sm.a_full[as], (uint32_t)((ac / kAStages) & 1), fail) ||
               !wait_or_fail(&sm.b_full[bs], (uint32_t)((bc / kBStages) & 1), fail)) { ok = false; break; }
@@ -384,15 +394,14 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
           uint32_t const a0 = smem_u32(sm.A[as][0]), b0 = smem_u32(sm.B[bs][0]);
 #pragma unroll
           for (int ks = 0; ks < 2; ++ks) {
-            // hi.hi into the main accumulator, hi.lo and lo.hi into the
-            // correction accumulator; parts are kAPart*4 / kBPart*4 bytes
-            // apart, k-steps 2 core columns (2*16*128 / 2*20*128 bytes) apart
+            // hi.hi into the main buffer, hi.lo and lo.hi into the correction
+            // accumulator; parts are kAPart*4 / kBPart*4 bytes apart, k-steps
+            // 2 core columns (2*16*128 / 2*20*128 bytes) apart
             uint32_t const ak = a0 + ks * 2 * (kM / 8) * 128, bk = b0 + ks * 2 * (kBtN / 8) * 128;
             uint64_t const ahi = sdesc(ak, (kM / 8) * 128, 128), alo = sdesc(ak + kAPart * 4, (kM / 8) * 128, 128);
             uint64_t const bhi = sdesc(bk, (kBtN / 8) * 128, 128), blo = sdesc(bk + kBPart * 4, (kBtN / 8) * 128, 128);
-            uint32_t const acc = (c | ks) ? 1u : 0u;
-            mma_tf32(d, ahi, bhi, acc);
-            mma_tf32(dc, ahi, blo, acc);
+            mma_tf32(d, ahi, bhi, ((c % kHalf) | ks) ? 1u : 0u);
+            mma_tf32(dc, ahi, blo, (c | ks) ? 1u : 0u);
             mma_tf32(dc, alo, bhi, 1u);
           }
           mma_any = true;
@@ -400,7 +409,7 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
           mma_commit(&sm.b_empty[bs]);
         }
         if (!ok) break;
-        mma_commit(&sm.acc_full[buf]);
+        mma_commit(&sm.acc_full);
       }
     }
   } else if (warp < kWarpE0) {
@@ -522,25 +531,25 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
 #pragma unroll
           for (int k = 0; k < HLBL_QED_NW; ++k) q.w[e][k] = (float)wq[((size_t)vv * 3 + e) * HLBL_QED_NW + k];
       }
-      int const buf = P % kAcc;
-      if (!wait_or_fail(&sm.acc_full[buf], (uint32_t)((P / kAcc) & 1), fail)) break;
+      if (!wait_or_fail(&sm.acc_full, (uint32_t)(P & 1), fail)) break;
       tc_fence_after();
-      uint32_t const c0 = (uint32_t)(buf * kBtN);
-      // fold the corrections into the main accumulator, then free them
+      uint32_t const c0 = (uint32_t)((P & 1) * kBtN), c1 = (uint32_t)(((P + 1) & 1) * kBtN);
+      // fold the second half and the corrections into the first half
 #pragma unroll 1
       for (int jj = 0; jj < 10; ++jj) {
-        float m[16], k[16];
+        float m[16], h[16], k[16];
         tmem_ld16(lane_addr + c0 + 16 * jj, m);
+        tmem_ld16(lane_addr + c1 + 16 * jj, h);
         tmem_ld16(lane_addr + kCorrCol + 16 * jj, k);
         tmem_wait_ld();
 #pragma unroll
-        for (int i = 0; i < 16; ++i) m[i] += k[i];
+        for (int i = 0; i < 16; ++i) m[i] = (m[i] + h[i]) + k[i];
         tmem_st16(lane_addr + c0 + 16 * jj, m);
       }
       tmem_wait_st();
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(&sm.corr_empty);
+      if (lane == 0) mbar_arrive(&sm.folded);
       tc_fence_after();
       float a;
       switch (quad) {
@@ -551,7 +560,7 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(&sm.acc_empty[buf]);
+      if (lane == 0) mbar_arrive(&sm.dotted);
       if (valid) {
         if (P & 1) run1.add(-(double)a);
         else run0.add(-(double)a);

@@ -40,7 +40,7 @@ constexpr int WPAD = H + 8;  // BF16 row stride of the resident weights (bank sp
 __constant__ float c_base_node[8];
 __constant__ float c_base_weight[8];
 
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 __device__ __forceinline__ float dsilu(float z) {
   float const s = 1.0f / (1.0f + __expf(-z));
   return s * (1.0f + z * (1.0f - s));

@@ -119,6 +119,12 @@ int hlbl_autotune(hlbl_ctx* ctx, const double* d_fwd_y, int n, const double* con
                   const int* gsx, const int* yv, double xunit, double* d_out, int* best_p1,
                   int* best_p2, int* best_group, double* best_ms);
 
+/* Exact QED weight of the FP32 path: the quadrature in FP32 where
+ * min(|x|, |y|) >= r64 (units of 1/m_mu) and in FP64 inside (on = 1, the
+ * default, r64 = 0.1), or FP64 everywhere (on = 0). The FP64 path always
+ * evaluates it in FP64. No counterpart in the reference. */
+int hlbl_ctx_set_qed_fp32(hlbl_ctx* ctx, int on, double r64);
+
 /* FP32 two-flavour pass 2 on the tensor cores (on = 1, the default:
  * tcgen05 MMAs with 3xTF32 products, FP32 tile copies of the blocks written
  * by pass 1) or on the CUDA cores (on = 0). No counterpart in the

@@ -67,3 +67,28 @@ def test_tensor_core_batched_equals_per_pair():
             assert S.pair_rel_err(got[i], one) <= 1e-5
             orc = S.oracle_kernel_sum(srcs[i], y, gsxs[i], yvs[i], xu, lat)
             assert S.pair_rel_err(got[i], orc) <= TOL32
+
+
+def test_fp32_quadrature_weight_matches_fp64_weight():
+    """The mixed path's exact QED weight in FP32 (FP64 within r64 of the
+    origin) against the FP64 weight everywhere: the same kernel sums to FP32
+    accuracy (every quadrature term is positive). With r64 larger than the
+    lattice, every row takes the FP64 branch and the sums are identical."""
+    import hlbl_gb300 as hg
+
+    lat = (8, 6, 6, 6)
+    xu = hg.xunit(105.658, 0.1)
+    src, y = S.gaussian_block(lat, 51), S.gaussian_block(lat, 52)
+    gsx, yv = (2, 1, 0, 5), (2, -2, 1, 0)
+    orc = S.oracle_kernel_sum(src, y, gsx, yv, xu, lat)
+    with hg.Contractor(lat) as c:
+        d_src, d_y = dev(src), dev(y)
+        c.set_qed_fp32(False)
+        w64 = c.kernel_sum(d_src, d_y, gsx, yv, xu, hg.FP32)
+        c.set_qed_fp32(True, 0.1)
+        w32 = c.kernel_sum(d_src, d_y, gsx, yv, xu, hg.FP32)
+        c.set_qed_fp32(True, 1e3)
+        w32_all64 = c.kernel_sum(d_src, d_y, gsx, yv, xu, hg.FP32)
+    assert w32_all64 == w64
+    assert S.pair_rel_err(w32, w64) <= 1e-6
+    assert S.pair_rel_err(w32, orc) <= TOL32
