@@ -66,6 +66,7 @@ def _load() -> C.CDLL:
                                                C.c_double, C.c_int, vp]),
         "hlbl_ctx_set_batch_group": (C.c_int, [vp, C.c_int]),
         "hlbl_ctx_set_tensor_cores": (C.c_int, [vp, C.c_int]),
+        "hlbl_f32_tile_copy": (C.c_int, [vp, vp, vp]),
         "hlbl_ctx_set_qed_fp32": (C.c_int, [vp, C.c_int, C.c_double]),
         "hlbl_ctx_reserve": (C.c_int, [vp, C.c_int]),
         "hlbl_stage_async": (C.c_int, [vp, vp, vp, C.c_size_t, C.c_int]),

@@ -172,6 +172,10 @@ class Contractor:
         (FP64 inside), or FP64 everywhere."""
         check(lib.hlbl_ctx_set_qed_fp32(self._h, 1 if on else 0, float(r64)))
 
+    def f32_tile_copy(self, d_block, d_out) -> None:
+        """The FP32 tile copy of a block (the tensor-core pass 2's input layout)."""
+        check(lib.hlbl_f32_tile_copy(self._h, ptr(d_block), ptr(d_out)))
+
     def set_tensor_cores(self, on: bool) -> None:
         """FP32 two-flavour pass 2 on the tensor cores (default) or the CUDA cores."""
         check(lib.hlbl_ctx_set_tensor_cores(self._h, 1 if on else 0))

@@ -103,6 +103,22 @@ __global__ void wait_timeout_selftest_kernel(int* err) {
   if (!ok && threadIdx.x == 0) atomicExch(err, kErrWaitTimeout);
 }
 
+// The FP32 tile copy of one block ([f][ia][tile][6][32][4] floats), with the
+// conversion pass 1 uses; sites past V in the last tile are left untouched.
+__global__ void f32_tile_copy_kernel(const double* __restrict__ blk, Geometry geo, float* __restrict__ out) {
+  long long const n = geo.V * 24 * 6;  // (f, ia, site, c4)
+  long long const nt32 = (geo.V + 31) / 32;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    int const c4 = (int)(i % 6);
+    long long const site = (i / 6) % geo.V;
+    int const row = (int)(i / (6 * geo.V));  // f*12 + ia
+    const double* src = blk + ((size_t)row * geo.V + site) * 24 + 4 * c4;
+    float4 const v = make_float4(f64_to_f32(src[0]), f64_to_f32(src[1]), f64_to_f32(src[2]), f64_to_f32(src[3]));
+    *reinterpret_cast<float4*>(out + ((size_t)row * nt32 + (site >> 5)) * (32 * 24) + c4 * 128 + (site & 31) * 4) = v;
+  }
+}
+
 // ---- launch plumbing -------------------------------------------------------
 template <typename T, int NF, int TS>
 struct P1Launch {
@@ -111,6 +127,10 @@ struct P1Launch {
   static int init(int nsm, int& grid) {
     cudaError_t e = cudaFuncSetAttribute(p1_kernel<T, NF, TS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // all of the unified L1/shared storage as shared memory: two FP32 CTAs per SM
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(p1_kernel<T, NF, TS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return cuda_fail(e, "p1 smem attribute");
     int nb = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, p1_kernel<T, NF, TS>, threads, smem);
@@ -576,6 +596,13 @@ int hlbl_kernel_sums_batched(hlbl_ctx* c, const double* y, int n, const double* 
     if (int rc = run_pass2(c, c->geo, y, b, xunit, 0, 2, precision, 0)) return rc;
   }
   return check_launch("hlbl_kernel_sums_batched launch");
+}
+
+int hlbl_f32_tile_copy(hlbl_ctx* c, const double* d_block, float* d_out) {
+  if (!c || !d_block || !d_out) return fail(HLBL_EINVAL, "hlbl_f32_tile_copy: null argument");
+  if (!aligned16(d_block) || !aligned16(d_out)) return fail(HLBL_EINVAL, "hlbl_f32_tile_copy: pointers must be 16-byte aligned");
+  f32_tile_copy_kernel<<<c->nsm * 8, 256, 0, c->stream>>>(d_block, c->geo, d_out);
+  return check_launch("hlbl_f32_tile_copy launch");
 }
 
 int hlbl_ctx_set_qed_fp32(hlbl_ctx* c, int on, double r64) {

@@ -54,11 +54,35 @@ struct Neu {
 // convert each landed tile once into an FP32 copy, then re-use the stage
 // for the next tile's TMA while computing on the copy (an FP64 -> FP32
 // conversion issues on the FP64 pipe, so converting at every use is slow).
+// Row stride of a staged tile in the compute type: FP64 stages are the TMA
+// target, TS*24 dense; the FP32 copy pads each row by 16 bytes, so that the
+// rows threads of one warp read start in different banks.
+template <typename T, int TS>
+constexpr int row_stride() { return sizeof(T) == sizeof(double) ? TS * 24 : TS * 24 + 4; }
+
 template <typename T, int NF, int TS>
 constexpr size_t stage_bytes() {
   return sizeof(T) == sizeof(double)
              ? sizeof(double) * (size_t)(2 * 2 * NF * 12 * TS * 24)
-             : sizeof(double) * (size_t)(2 * NF * 12 * TS * 24) + sizeof(float) * (size_t)(2 * NF * 12 * TS * 24);
+             : sizeof(double) * (size_t)(2 * NF * 12 * TS * 24) +
+                   sizeof(float) * (size_t)(2 * NF * 12 * row_stride<float, TS>());
+}
+
+// FP64 -> FP32, rounded to nearest even, on the integer pipe (the conversion
+// instruction issues on GB300's FP64 pipe): the exponent rebased, the top 23
+// of the 52 mantissa bits, plus the increment that the 29 dropped bits call
+// for (the carry may run into the exponent, as rounding requires). Zeros,
+// values outside FP32's normal range, infinities and NaNs take the
+// conversion instruction.
+__device__ __forceinline__ float f64_to_f32(double d) {
+  unsigned long long const b = (unsigned long long)__double_as_longlong(d);
+  uint32_t const hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+  uint32_t const e = (hi >> 20) & 0x7FFu;
+  if (e - 897u > 253u) return __double2float_rn(d);
+  uint32_t r = ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+  uint32_t const rest = lo & 0x1FFFFFFFu;
+  r += (uint32_t)(rest > 0x10000000u) | ((uint32_t)(rest == 0x10000000u) & (r & 1u));
+  return __uint_as_float((hi & 0x80000000u) | r);
 }
 
 // TMA staging of one tile: rows (which, fl, ia) of the two blocks, the
@@ -81,15 +105,33 @@ __device__ __forceinline__ void issue_tile(double* stage, uint64_t* bar, const d
   }
 }
 
-// Convert a landed FP64 stage into the FP32 compute copy (all threads).
+// Convert a landed FP64 stage into the FP32 compute copy (all threads),
+// rows at stride row_stride<float, TS>().
 template <int NF, int TS>
 __device__ __forceinline__ void convert_stage(const double* __restrict__ st, float* __restrict__ cp) {
-  constexpr int kN = 2 * NF * 12 * TS * 24 / 2;
+  constexpr int kRowPairs = TS * 24 / 2, RS = row_stride<float, TS>();
+  constexpr int kN = 2 * NF * 12 * kRowPairs;
   const double2* s2 = reinterpret_cast<const double2*>(st);
-  float2* c2 = reinterpret_cast<float2*>(cp);
   for (int i = threadIdx.x; i < kN; i += blockDim.x) {
     double2 const v = s2[i];
-    c2[i] = make_float2((float)v.x, (float)v.y);
+    int const row = i / kRowPairs, k = i % kRowPairs;
+    *reinterpret_cast<float2*>(cp + row * RS + 2 * k) = make_float2(f64_to_f32(v.x), f64_to_f32(v.y));
+  }
+}
+
+// A site's 24 components from a staged row into registers (16-byte loads).
+__device__ __forceinline__ void load_row(const float* __restrict__ p, float r[24]) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    float4 const v = reinterpret_cast<const float4*>(p)[i];
+    r[4 * i] = v.x; r[4 * i + 1] = v.y; r[4 * i + 2] = v.z; r[4 * i + 3] = v.w;
+  }
+}
+__device__ __forceinline__ void load_row(const double* __restrict__ p, double r[24]) {
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    double2 const v = reinterpret_cast<const double2*>(p)[i];
+    r[2 * i] = v.x; r[2 * i + 1] = v.y;
   }
 }
 
@@ -113,7 +155,8 @@ __device__ __forceinline__ void write_f32_tiles(const float* __restrict__ cp, fl
     int const f = which == 0 ? f0 + fl : 1 - f0 - fl;
     long long const v = s0 + s;
     size_t const off = ((size_t)(f * 12 + ia) * nt32 + (size_t)(v >> 5)) * (32 * 24) + c4 * 128 + (v & 31) * 4;
-    *reinterpret_cast<float4*>(dst + off) = *reinterpret_cast<const float4*>(cp + ((size_t)row * TS + s) * 24 + c4 * 4);
+    *reinterpret_cast<float4*>(dst + off) =
+        *reinterpret_cast<const float4*>(cp + (size_t)row * row_stride<float, TS>() + s * 24 + c4 * 4);
   }
 }
 
@@ -131,7 +174,7 @@ __device__ __forceinline__ void write_f32_tiles(const float* __restrict__ cp, fl
 // tile copies the tensor-core pass 2 reads (y32 by pair 0's CTAs, each
 // partner's by its own; null pointers: no copy).
 template <typename T, int NF, int TS>
-__global__ void __launch_bounds__(NF * 144)
+__global__ void __launch_bounds__(NF * 144, sizeof(T) == sizeof(float) ? 2 : 1)
 p1_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, int f0,
           double* __restrict__ partials, int* __restrict__ err, float* __restrict__ y32) {
   constexpr int kRows = 2 * NF * 12;
@@ -229,12 +272,22 @@ p1_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, int f0,
       write_f32_tiles<NF, TS>(s_copy, batch.p[pi].src32, pi == 0 ? y32 : nullptr, f0, geo.V, s0, nvalid);
     }
 
-    const T* A_base = tile_data + ((size_t)(0 * NF + fl) * 12 + ia) * TS * 24;
-    const T* B_base = tile_data + ((size_t)(1 * NF + fl) * 12 + ib) * TS * 24;
+    constexpr int RS = row_stride<T, TS>();
+    const T* A_base = tile_data + ((size_t)(0 * NF + fl) * 12 + ia) * RS;
+    const T* B_base = tile_data + ((size_t)(1 * NF + fl) * 12 + ib) * RS;
 #pragma unroll 1
     for (int s = 0; s < nvalid; ++s) {
+      // FP32: the site's rows into registers with 16-byte loads; FP64: read
+      // in place (two rows of doubles would crowd the registers)
+      T Ar[24], Br[24];
       const T* A = A_base + s * 24;
       const T* B = B_base + s * 24;
+      if constexpr (sizeof(T) == sizeof(float)) {
+        load_row(A, Ar);
+        load_row(B, Br);
+        A = Ar;
+        B = Br;
+      }
       // P[s1][s2] for s2 = s1^2 (gamma_0, gamma_3) and s2 = 3-s1 (gamma_1, gamma_2)
       T pa[4][2], pb[4][2];
 #pragma unroll
@@ -687,8 +740,9 @@ p2_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, P2Args ar
     // D_mu[p][q] for every site and flavour (zero past the tile's valid sites)
     for (int it = t; it < TS * NF * 144; it += nthr) {
       int const s = it / (NF * 144), fl = (it / 144) % NF, pq = it % 144, p = pq / 12, q = pq % 12;
-      const T* S = tile_data + ((size_t)(0 * NF + fl) * 12 + q) * TS * 24 + s * 24;
-      const T* Y = tile_data + ((size_t)(1 * NF + fl) * 12 + p) * TS * 24 + s * 24;
+      constexpr int RS = row_stride<T, TS>();
+      const T* S = tile_data + ((size_t)(0 * NF + fl) * 12 + q) * RS + s * 24;
+      const T* Y = tile_data + ((size_t)(1 * NF + fl) * 12 + p) * RS + s * 24;
       if (s >= nvalid) {
         T* Dz = s_D + ((size_t)(s * NF + fl) * 4) * kBtK + 2 * (p * 12 + q);
 #pragma unroll

@@ -119,6 +119,14 @@ int hlbl_autotune(hlbl_ctx* ctx, const double* d_fwd_y, int n, const double* con
                   const int* gsx, const int* yv, double xunit, double* d_out, int* best_p1,
                   int* best_p2, int* best_group, double* best_ms);
 
+/* The FP32 tile copy of a block that pass 1 of the FP32 path writes and the
+ * tensor-core pass 2 reads: d_out[f][ia][tile][6][32][4] floats, tiles of 32
+ * sites ((V + 31) / 32 of them, the last padded and its pad left untouched),
+ * a site's 24 sink components as six groups of 4; each value rounded to
+ * nearest even from FP64. Asynchronous on the context's stream. No
+ * counterpart in the reference. */
+int hlbl_f32_tile_copy(hlbl_ctx* ctx, const double* d_block, float* d_out);
+
 /* Exact QED weight of the FP32 path: the quadrature in FP32 where
  * min(|x|, |y|) >= r64 (units of 1/m_mu) and in FP64 inside (on = 1, the
  * default, r64 = 0.1), or FP64 everywhere (on = 0). The FP64 path always

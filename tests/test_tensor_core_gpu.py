@@ -92,3 +92,30 @@ def test_fp32_quadrature_weight_matches_fp64_weight():
     assert w32_all64 == w64
     assert S.pair_rel_err(w32, w64) <= 1e-6
     assert S.pair_rel_err(w32, orc) <= TOL32
+
+
+def test_f32_tile_copy_rounds_like_ieee_and_lays_out_tiles():
+    """The FP64 -> FP32 conversion of pass 1 (integer pipe, round to nearest
+    even) against numpy's IEEE conversion, bit for bit, on Gaussian values
+    and planted edge cases (ties, zeros, subnormals, overflow, infinities);
+    and the tile layout [f][ia][tile][6][32][4] with a ragged last tile."""
+    import hlbl_gb300 as hg
+
+    lat = (3, 5, 1, 7)  # V = 105: four tiles of 32, the last one ragged
+    V = S.volume(lat)
+    blk = S.gaussian_block(lat, 61)
+    edge = np.array([0.0, -0.0, 1.0 + 2.0 ** -24, 1.0 + 3 * 2.0 ** -24, -(1.0 + 2.0 ** -24), 1e-40, -3e-39,
+                     1e-50, 3.5e38, -3.5e38, 3.4028235677973366e38, np.inf, -np.inf, 1.17549435e-38,
+                     2.0 ** -126 * (1 - 2.0 ** -25), 65504.0 + 2.0 ** -13])
+    blk[:edge.size] = edge
+    blk[1000:1000 + edge.size] = edge * 3.0
+    nt = (V + 31) // 32
+    out = torch.full((2 * 12 * nt * 768,), float("nan"), dtype=torch.float32, device="cuda")
+    with hg.Contractor(lat) as c:
+        c.f32_tile_copy(dev(blk), out)
+        c.check()
+    got = out.cpu().numpy().reshape(2 * 12, nt, 6, 32, 4)
+    want = blk.astype(np.float32).reshape(2 * 12, V, 6, 4)
+    for site in range(V):
+        a = got[:, site // 32, :, site % 32, :]
+        assert np.array_equal(a.view(np.uint32), want[:, site].view(np.uint32)), site
