@@ -10,6 +10,8 @@
 // bytes, so every tile load is a set of 48 contiguous 16-byte-aligned runs.
 #pragma once
 
+#include <type_traits>
+
 #include "hlbl_device.cuh"
 
 namespace hg {
@@ -47,6 +49,20 @@ struct Neu {
     s = t;
   }
   __device__ __forceinline__ double get() const { return s + c; }
+};
+
+// Kahan's compensated FP32 sum (s - c is the sum): the FP32 path's per-thread
+// sums over its tiles, kept off GB300's FP64 pipe (1/64 of the FP32 rate)
+// until the end.
+struct KahanF {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    float const y = v - c;
+    float const t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double get() const { return (double)s - (double)c; }
 };
 
 // Input staging: FP64 kernels double-buffer the FP64 tile (TMA into one
@@ -181,7 +197,9 @@ p1_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, int f0,
   constexpr size_t kStage = (size_t)kRows * TS * 24;  // doubles per stage
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double* s_stage = reinterpret_cast<double*>(smem_raw);         // [2][kRows][TS][24]
-  int* s_zh = reinterpret_cast<int*>(smem_raw + stage_bytes<T, NF, TS>());  // [TS][4]
+  // zerohalf weights of the tile's sites, converted once (a per-thread
+  // int -> float conversion issues on GB300's slow FP64/conversion pipe)
+  T* s_zh = reinterpret_cast<T*>(smem_raw + stage_bytes<T, NF, TS>());  // [TS][4]
   __shared__ __align__(8) uint64_t s_bar[2];
   __shared__ int s_fail;
 
@@ -191,34 +209,32 @@ p1_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, int f0,
   int const t = threadIdx.x;
   int const fl = t / 144, ia = (t % 144) / 12, ib = t % 12;
 
-  // FP64 per-thread sums over this CTA's tiles: compensated on the FP64
-  // path, plain on the FP32 path (whose tile sums are only FP32-accurate).
+  // Per-thread sums over this CTA's tiles, each tile's sum added in:
+  // compensated FP64 on the FP64 path, compensated FP32 (Kahan) on the FP32
+  // path, converted to FP64 at the end.
   constexpr bool kComp = sizeof(T) == sizeof(double);
-  Neu acc_u[6][2], acc_s[4][2];
+  using Acc = typename std::conditional<kComp, Neu, KahanF>::type;
+  Acc acc_u[6][2], acc_s[4][2];
   T tu[6][2], ts[4][2];
 #pragma unroll
   for (int k = 0; k < 6; ++k) tu[k][0] = tu[k][1] = T(0);
 #pragma unroll
   for (int s = 0; s < 4; ++s) ts[s][0] = ts[s][1] = T(0);
-  int pending_sites = 0;
   auto flush = [&]() {
 #pragma unroll
     for (int k = 0; k < 6; ++k)
 #pragma unroll
       for (int e = 0; e < 2; ++e) {
-        if (kComp) acc_u[k][e].add((double)tu[k][e]);
-        else acc_u[k][e].s += (double)tu[k][e];
+        acc_u[k][e].add(tu[k][e]);
         tu[k][e] = T(0);
       }
 #pragma unroll
     for (int s = 0; s < 4; ++s)
 #pragma unroll
       for (int e = 0; e < 2; ++e) {
-        if (kComp) acc_s[s][e].add((double)ts[s][e]);
-        else acc_s[s][e].s += (double)ts[s][e];
+        acc_s[s][e].add(ts[s][e]);
         ts[s][e] = T(0);
       }
-    pending_sites = 0;
   };
 
   constexpr bool kDB = sizeof(T) == sizeof(double);  // double-buffered FP64 stages
@@ -251,7 +267,7 @@ p1_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, int f0,
       int rel[4];
       rel_coords(geo, gsx, min(s0 + s, geo.V - 1), rel);
 #pragma unroll
-      for (int r = 0; r < 4; ++r) s_zh[s * 4 + r] = coord_map_zerohalf(rel[r], geo.global[r]);
+      for (int r = 0; r < 4; ++r) s_zh[s * 4 + r] = (T)coord_map_zerohalf(rel[r], geo.global[r]);
     }
     uint32_t const parity = kDB ? (uint32_t)((i >> 1) & 1) : (uint32_t)(i & 1);
     if (!mbar_wait(&s_bar[st], parity)) s_fail = 1;
@@ -317,7 +333,7 @@ p1_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, int f0,
         }
         X[sg][0] = xr; X[sg][1] = xi;
       }
-      const int* zh = s_zh + s * 4;
+      const T* zh = s_zh + s * 4;
 #pragma unroll
       for (int sg = 0; sg < 4; ++sg) { ts[sg][0] += X[sg][0]; ts[sg][1] += X[sg][1]; }
 #pragma unroll
@@ -328,9 +344,7 @@ p1_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, int f0,
         tu[k][1] += wr * X[g][1] - wg * X[r][1];
       }
     }
-    pending_sites += nvalid;
-    // FP64 path: every tile; FP32 path: every >= 32 sites
-    if (kComp || pending_sites >= 32) flush();
+    flush();
     __syncthreads();
   }
   flush();
@@ -603,7 +617,7 @@ constexpr size_t p2_smem_bytes() {
 
 template <typename T, int NF, int TS>
 constexpr size_t p1_smem_bytes() {
-  return stage_bytes<T, NF, TS>() + sizeof(int) * TS * 4;
+  return stage_bytes<T, NF, TS>() + sizeof(T) * TS * 4;
 }
 
 // The pass-1 variant of hlbl_cu_dzu_dzsu_noalloc: one flavour, FP64, the

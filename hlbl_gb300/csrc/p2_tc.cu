@@ -263,7 +263,7 @@ __device__ __forceinline__ float dot_zh(const float* G, const SiteQ& q) {
 // One phase's row: sum_n coef[MU][n] F[n], F at column c of this warp's lane
 // quadrant (16 columns = one 4 x 4 matrix per j).
 template <int MU>
-__device__ __noinline__ float epilogue_row(uint32_t lane_addr, uint32_t c, const SiteQ& q) {
+__device__ __forceinline__ float epilogue_row(uint32_t lane_addr, uint32_t c, const SiteQ& q) {
   float f[16], a = 0.f;
 #define HG_TC_K(J)                      \
   tmem_ld16(lane_addr + c + 16 * J, f); \
