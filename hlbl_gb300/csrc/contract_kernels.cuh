@@ -151,28 +151,33 @@ __device__ __forceinline__ void load_row(const double* __restrict__ p, double r[
   }
 }
 
-// Write a converted tile's rows into the FP32 tile copies ([f][ia][tile32]
-// [6][32][4] floats, 32-site tiles): rows of `a` (flavour f0 + fl) into a32,
-// rows of `b` (flavour 1 - f0 - fl) into b32; consecutive threads write
-// consecutive 16-byte groups of one row.
+// Pass 1's FP32 path: convert a landed FP64 stage into the FP32 compute copy
+// and, in the same pass, into the FP32 tile copies (y32 by pair 0's CTAs).
+// One unit = (row, 16-byte group c4, site); consecutive threads take
+// consecutive sites, so the global stores of 8 threads cover 128 contiguous
+// bytes.
 template <int NF, int TS>
-__device__ __forceinline__ void write_f32_tiles(const float* __restrict__ cp, float* __restrict__ a32,
-                                                float* __restrict__ b32, int f0, long long V, long long s0,
-                                                int nvalid) {
+__device__ __forceinline__ void convert_and_copy(const double* __restrict__ st, float* __restrict__ cp,
+                                                 float* __restrict__ a32, float* __restrict__ b32, int f0,
+                                                 long long V, long long s0, int nvalid) {
   static_assert(32 % TS == 0, "a tile lies inside one 32-site tile of the copy");
-  if (a32 == nullptr && b32 == nullptr) return;
+  constexpr int kRows = 2 * NF * 12, RS = row_stride<float, TS>();
   long long const nt32 = (V + 31) / 32;
-  int const n = 2 * NF * 12 * 6 * nvalid;
-  for (int it = threadIdx.x; it < n; it += blockDim.x) {
-    int const s = it % nvalid, rem = it / nvalid, c4 = rem % 6, row = rem / 6;
+  for (int u = threadIdx.x; u < kRows * 6 * TS; u += blockDim.x) {
+    int const si = u % TS, c4 = (u / TS) % 6, row = u / (6 * TS);
+    if (si >= nvalid) continue;
+    const double2* src = reinterpret_cast<const double2*>(st + ((size_t)row * TS + si) * 24 + 4 * c4);
+    double2 const v0 = src[0], v1 = src[1];
+    float4 const f = make_float4(f64_to_f32(v0.x), f64_to_f32(v0.y), f64_to_f32(v1.x), f64_to_f32(v1.y));
+    *reinterpret_cast<float4*>(cp + (size_t)row * RS + si * 24 + 4 * c4) = f;
     int const which = row / (NF * 12), fl = (row / 12) % NF, ia = row % 12;
     float* dst = which == 0 ? a32 : b32;
-    if (dst == nullptr) continue;
-    int const f = which == 0 ? f0 + fl : 1 - f0 - fl;
-    long long const v = s0 + s;
-    size_t const off = ((size_t)(f * 12 + ia) * nt32 + (size_t)(v >> 5)) * (32 * 24) + c4 * 128 + (v & 31) * 4;
-    *reinterpret_cast<float4*>(dst + off) =
-        *reinterpret_cast<const float4*>(cp + (size_t)row * row_stride<float, TS>() + s * 24 + c4 * 4);
+    if (dst != nullptr) {
+      int const ff = which == 0 ? f0 + fl : 1 - f0 - fl;
+      long long const v = s0 + si;
+      *reinterpret_cast<float4*>(dst + ((size_t)(ff * 12 + ia) * nt32 + (size_t)(v >> 5)) * (32 * 24) +
+                                 c4 * 128 + (v & 31) * 4) = f;
+    }
   }
 }
 
@@ -278,14 +283,14 @@ p1_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, int f0,
       tile_data = reinterpret_cast<const T*>(s_stage + st * kStage);
     } else {
       // FP32: convert once, then the stage takes the next tile while we compute
-      convert_stage<NF, TS>(s_stage, s_copy);
+      convert_and_copy<NF, TS>(s_stage, s_copy, batch.p[pi].src32, pi == 0 ? y32 : nullptr, f0, geo.V, s0,
+                               nvalid);
       __syncthreads();
       if (t == 0 && next_in_flight) {
         fence_proxy_async_smem();
         issue_tile<NF, TS>(s_stage, &s_bar[0], src, y, f0, 1, 1 - f0, -1, geo.V, (tile + gridDim.x) * TS);
       }
       tile_data = reinterpret_cast<const T*>(s_copy);
-      write_f32_tiles<NF, TS>(s_copy, batch.p[pi].src32, pi == 0 ? y32 : nullptr, f0, geo.V, s0, nvalid);
     }
 
     constexpr int RS = row_stride<T, TS>();

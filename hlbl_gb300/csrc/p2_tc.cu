@@ -15,10 +15,11 @@
 //          rows p: 3 KB per (flavour, ia, tile)) -- one thread
 //   1      TMA producer of the B chunks (16 k x 160 n, hi and lo, 20 KB) -- one thread
 //   2      TMEM allocation; tcgen05.mma issue and commits -- one thread
-//   3-10   D formation: per chunk of 16 k (8 (p, q)), warp w forms (p, q) =
-//          the chunk's w-th for its lane's site: O = Y conj(S) spin blocks
-//          -> D_mu -> hi/lo -> shared memory in the K-major no-swizzle
-//          core-matrix layout
+//   3-10   D formation, two groups of four warps on alternate chunks of
+//          16 k (8 (p, q)): warp j of a group forms the chunk's j-th pair of
+//          (p, q) (one Y row, two S rows) for its lane's site: O = Y conj(S)
+//          spin blocks -> D_mu -> hi/lo -> shared memory in the K-major
+//          no-swizzle core-matrix layout
 //   11-14  epilogue: one TMEM lane quadrant each (warp % 4 = mu); per phase,
 //          the F rows from TMEM dotted with the QED coefficients of the
 //          row's site, into a compensated FP64 sum
@@ -63,6 +64,7 @@ constexpr uint32_t kCorrCol = 2 * kBtN;          // the correction accumulator's
 constexpr int kAPart = kM * kKc;           // floats per A part (hi or lo)
 constexpr int kBPart = kBtN * kKc;         // floats per B part
 constexpr int kWarpRows = 0, kWarpB = 1, kWarpMma = 2, kWarpD0 = 3, kDWarps = 8;
+constexpr int kDGroup = 4;  // D warps per chunk (a group); kDWarps / kDGroup chunks in flight
 constexpr int kWarpE0 = kWarpD0 + kDWarps, kEWarps = 4;
 constexpr int kThreads = 32 * (kWarpE0 + kEWarps);
 constexpr uint32_t kTmemCols = 512;
@@ -301,7 +303,7 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
   if (t == 0) {
     for (int i = 0; i < 2; ++i) { mbar_init(&sm.s_full[i], 1); mbar_init(&sm.s_empty[i], kDWarps); }
     for (int i = 0; i < kYSlots; ++i) { mbar_init(&sm.y_full[i], 1); mbar_init(&sm.y_empty[i], kDWarps); }
-    for (int i = 0; i < kAStages; ++i) { mbar_init(&sm.a_full[i], kDWarps); mbar_init(&sm.a_empty[i], 1); }
+    for (int i = 0; i < kAStages; ++i) { mbar_init(&sm.a_full[i], kDGroup); mbar_init(&sm.a_empty[i], 1); }
     for (int i = 0; i < kBStages; ++i) { mbar_init(&sm.b_full[i], 1); mbar_init(&sm.b_empty[i], 1); }
     mbar_init(&sm.acc_full, 1);
     mbar_init(&sm.folded, kEWarps);
@@ -349,7 +351,10 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
           mbar_arrive_expect_tx(&sm.y_full[slot], kRowBytes);
           bulk_g2s(sm.Y[slot], row_ptr(y32, f, p, tile), kRowBytes, &sm.y_full[slot]);
           rows_issued_y = uy;
-          if (p == 1 && P + 1 < nph) ok = issue_S(P + 1);
+          // the next phase's S rows into the other buffer, once its readers
+          // (the previous phase) are done: issuing Y[4] needed Y[0] of this
+          // phase consumed, so that wait no longer blocks the Y rows
+          if (p == kYSlots && P + 1 < nph) ok = issue_S(P + 1);
         }
       }
     }
@@ -414,9 +419,9 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
     }
   } else if (warp < kWarpE0) {
     // ---- D formation ----------------------------------------------------------------
-    int const j = warp - kWarpD0;  // the chunk's (p, q) this warp forms
+    int const grp = (warp - kWarpD0) / kDGroup;  // chunks c = grp, grp + 2, ...
+    int const j = (warp - kWarpD0) % kDGroup;    // the chunk's j-th pair of (p, q)
     int const s = lane;
-    int ac = 0;
     bool ok = true;
     for (int P = 0; ok && P < nph; ++P) {
       long long const tile = blockIdx.x + (long long)(P >> 1) * gridDim.x;
@@ -424,74 +429,92 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
       if (!wait_or_fail(&sm.s_full[P & 1], (uint32_t)((P >> 1) & 1), fail)) break;
       const float* Sb = sm.S[P & 1][0];
       int pw = -1;  // Y rows of this phase waited for
-      for (int c = 0; c < kChunks; ++c, ++ac) {
+      for (int c = grp; c < kChunks; c += kDWarps / kDGroup) {
         int const pmax = (8 * c + 7) / 12;
         while (ok && pw < pmax) {
           ++pw;
           ok = wait_or_fail(&sm.y_full[pw % kYSlots], (uint32_t)(((P * 12 + pw) / kYSlots) & 1), fail);
         }
-        int const as = ac % kAStages;
+        int const ac = P * kChunks + c, as = ac % kAStages;
         if (!ok || !wait_or_fail(&sm.a_empty[as], (uint32_t)(((ac / kAStages) & 1) ^ 1), fail)) { ok = false; break; }
-        int const pq = 8 * c + j, p = pq / 12, q = pq % 12;
-        // k = 2j + {re, im}: core column j/2, elements 2(j%2), 2(j%2)+1 of the
-        // row (mu*32 + s)
-        float* Ahi = sm.A[as][0] + (j >> 1) * 16 * 32 + s * 4 + 2 * (j & 1);
-        float* Alo = sm.A[as][1] + (j >> 1) * 16 * 32 + s * 4 + 2 * (j & 1);
+        int const pq0 = 8 * c + 2 * j, p = pq0 / 12, q0 = pq0 % 12;  // pq0, pq0 + 1 share p
+        // k = 4j .. 4j+3: core column j, the whole 16-byte row (mu*32 + s)
+        float* Ahi = sm.A[as][0] + j * 16 * 32 + s * 4;
+        float* Alo = sm.A[as][1] + j * 16 * 32 + s * 4;
         if (s < nvalid) {
           const float* Yr = sm.Y[p % kYSlots] + s * 4;
-          const float* Sr = Sb + q * kRowF32 + s * 4;
-          float y[24], x[24];
+          float y[24];
 #pragma unroll
           for (int c4 = 0; c4 < 6; ++c4) {
             float4 const a = *reinterpret_cast<const float4*>(Yr + c4 * 128);
-            float4 const b = *reinterpret_cast<const float4*>(Sr + c4 * 128);
             y[4 * c4] = a.x; y[4 * c4 + 1] = a.y; y[4 * c4 + 2] = a.z; y[4 * c4 + 3] = a.w;
-            x[4 * c4] = b.x; x[4 * c4 + 1] = b.y; x[4 * c4 + 2] = b.z; x[4 * c4 + 3] = b.w;
           }
-          // O[s1][s2] = sum_c Y[s1][c] conj(S[s2][c]), s2 = s1^2 (a) and 3-s1 (b)
-          float oa[4][2], ob[4][2];
+          float d[4][4];  // [mu][pq0 re, pq0 im, pq1 re, pq1 im]
 #pragma unroll
-          for (int s1 = 0; s1 < 4; ++s1) {
-            float ar = 0, ai = 0, br = 0, bi = 0;
+          for (int h = 0; h < 2; ++h) {
+            const float* Sr = Sb + (q0 + h) * kRowF32 + s * 4;
+            float x[24];
 #pragma unroll
-            for (int cc = 0; cc < 3; ++cc) {
-              float const yr = y[2 * (3 * s1 + cc)], yi = y[2 * (3 * s1 + cc) + 1];
-              int const sa = 2 * (3 * (s1 ^ 2) + cc), sb = 2 * (3 * (3 - s1) + cc);
-              ar += yr * x[sa] + yi * x[sa + 1];  ai += yi * x[sa] - yr * x[sa + 1];
-              br += yr * x[sb] + yi * x[sb + 1];  bi += yi * x[sb] - yr * x[sb + 1];
+            for (int c4 = 0; c4 < 6; ++c4) {
+              float4 const b = *reinterpret_cast<const float4*>(Sr + c4 * 128);
+              x[4 * c4] = b.x; x[4 * c4 + 1] = b.y; x[4 * c4 + 2] = b.z; x[4 * c4 + 3] = b.w;
             }
-            oa[s1][0] = ar; oa[s1][1] = ai; ob[s1][0] = br; ob[s1][1] = bi;
-          }
-#pragma unroll
-          for (int mu = 0; mu < 4; ++mu) {
-            float dr = 0, di = 0;
+            // O[s1][s2] = sum_c Y[s1][c] conj(S[s2][c]), s2 = s1^2 (a) and 3-s1 (b)
+            float oa[4][2], ob[4][2];
 #pragma unroll
             for (int s1 = 0; s1 < 4; ++s1) {
-              float const* o = (mu == 0 || mu == 3) ? oa[s1] : ob[s1];
-              float vr, vi;
-              mul_iph((6 - g5g_ph(mu, s1)) & 3, o[0], o[1], vr, vi);
-              dr += vr; di += vi;
+              float ar = 0, ai = 0, br = 0, bi = 0;
+#pragma unroll
+              for (int cc = 0; cc < 3; ++cc) {
+                float const yr = y[2 * (3 * s1 + cc)], yi = y[2 * (3 * s1 + cc) + 1];
+                int const sa = 2 * (3 * (s1 ^ 2) + cc), sb = 2 * (3 * (3 - s1) + cc);
+                ar += yr * x[sa] + yi * x[sa + 1];  ai += yi * x[sa] - yr * x[sa + 1];
+                br += yr * x[sb] + yi * x[sb + 1];  bi += yi * x[sb] - yr * x[sb + 1];
+              }
+              oa[s1][0] = ar; oa[s1][1] = ai; ob[s1][0] = br; ob[s1][1] = bi;
             }
-            float const hr = __uint_as_float(tf32_rna(dr)), hi_ = __uint_as_float(tf32_rna(di));
-            *reinterpret_cast<float2*>(Ahi + mu * 4 * 32) = make_float2(hr, hi_);
-            *reinterpret_cast<float2*>(Alo + mu * 4 * 32) =
-                make_float2(__uint_as_float(tf32_rna(dr - hr)), __uint_as_float(tf32_rna(di - hi_)));
+#pragma unroll
+            for (int mu = 0; mu < 4; ++mu) {
+              float dr = 0, di = 0;
+#pragma unroll
+              for (int s1 = 0; s1 < 4; ++s1) {
+                float const* o = (mu == 0 || mu == 3) ? oa[s1] : ob[s1];
+                float vr, vi;
+                mul_iph((6 - g5g_ph(mu, s1)) & 3, o[0], o[1], vr, vi);
+                dr += vr; di += vi;
+              }
+              d[mu][2 * h] = dr; d[mu][2 * h + 1] = di;
+            }
           }
-        } else {
-          float2 const z = make_float2(0.f, 0.f);
 #pragma unroll
           for (int mu = 0; mu < 4; ++mu) {
-            *reinterpret_cast<float2*>(Ahi + mu * 4 * 32) = z;
-            *reinterpret_cast<float2*>(Alo + mu * 4 * 32) = z;
+            float4 hi, lo;
+            hi.x = __uint_as_float(tf32_rna(d[mu][0])); hi.y = __uint_as_float(tf32_rna(d[mu][1]));
+            hi.z = __uint_as_float(tf32_rna(d[mu][2])); hi.w = __uint_as_float(tf32_rna(d[mu][3]));
+            lo.x = __uint_as_float(tf32_rna(d[mu][0] - hi.x)); lo.y = __uint_as_float(tf32_rna(d[mu][1] - hi.y));
+            lo.z = __uint_as_float(tf32_rna(d[mu][2] - hi.z)); lo.w = __uint_as_float(tf32_rna(d[mu][3] - hi.w));
+            *reinterpret_cast<float4*>(Ahi + mu * 4 * 32) = hi;
+            *reinterpret_cast<float4*>(Alo + mu * 4 * 32) = lo;
+          }
+        } else {
+          float4 const z = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+          for (int mu = 0; mu < 4; ++mu) {
+            *reinterpret_cast<float4*>(Ahi + mu * 4 * 32) = z;
+            *reinterpret_cast<float4*>(Alo + mu * 4 * 32) = z;
           }
         }
         fence_proxy_async_smem();
         __syncwarp();
         if (lane == 0) {
           mbar_arrive(&sm.a_full[as]);
-          // Y rows whose last chunk this was
-          for (int pp = (8 * c) / 12; pp <= pmax; ++pp)
-            if ((12 * pp + 11) / 8 == c) mbar_arrive(&sm.y_empty[pp % kYSlots]);
+          // Y rows whose last chunk in this group this was (each group
+          // arrives once per row: every row spans chunks of both groups)
+          for (int pp = (8 * c) / 12; pp <= pmax; ++pp) {
+            int const last = (12 * pp + 11) / 8;
+            int const last_g = last - ((last - grp) & 1);  // the group's last chunk using pp
+            if (last_g == c) mbar_arrive(&sm.y_empty[pp % kYSlots]);
+          }
         }
       }
       if (!ok) break;
