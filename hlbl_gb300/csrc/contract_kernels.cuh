@@ -84,21 +84,41 @@ constexpr size_t stage_bytes() {
                    sizeof(float) * (size_t)(2 * NF * 12 * row_stride<float, TS>());
 }
 
-// FP64 -> FP32, rounded to nearest even, on the integer pipe (the conversion
-// instruction issues on GB300's FP64 pipe): the exponent rebased, the top 23
-// of the 52 mantissa bits, plus the increment that the 29 dropped bits call
-// for (the carry may run into the exponent, as rounding requires). Zeros,
-// values outside FP32's normal range, infinities and NaNs take the
-// conversion instruction.
+// FP64 -> FP32, rounded to nearest even, on the integer pipe only (the
+// conversion instruction issues on GB300's FP64 pipe, 1/64 of the FP32
+// rate). Normal range: the exponent rebased, the top 23 of the 52 mantissa
+// bits, plus the increment the 29 dropped bits call for (a carry may run into
+// the exponent, as rounding requires; past the largest float it gives inf).
+// Outside it, also in integers: FP32 subnormals and zero (the 53-bit
+// significand shifted right with the same rounding), overflow to inf, inf and
+// NaN kept.
 __device__ __forceinline__ float f64_to_f32(double d) {
   unsigned long long const b = (unsigned long long)__double_as_longlong(d);
   uint32_t const hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+  uint32_t const sign = hi & 0x80000000u;
   uint32_t const e = (hi >> 20) & 0x7FFu;
-  if (e - 897u > 253u) return __double2float_rn(d);
-  uint32_t r = ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-  uint32_t const rest = lo & 0x1FFFFFFFu;
-  r += (uint32_t)(rest > 0x10000000u) | ((uint32_t)(rest == 0x10000000u) & (r & 1u));
-  return __uint_as_float((hi & 0x80000000u) | r);
+  if (e - 897u <= 253u) {
+    uint32_t r = ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    uint32_t const rest = lo & 0x1FFFFFFFu;
+    r += (uint32_t)(rest > 0x10000000u) | ((uint32_t)(rest == 0x10000000u) & (r & 1u));
+    return __uint_as_float(sign | r);
+  }
+  uint32_t r;
+  if (e == 0x7FFu) {
+    r = ((hi & 0xFFFFFu) | lo) ? 0x7FC00000u : 0x7F800000u;  // NaN (quiet) or inf
+  } else if (e > 1150u) {
+    r = 0x7F800000u;  // beyond the float range: inf
+  } else if (e < 873u) {
+    r = 0u;           // below half the smallest subnormal: zero
+  } else {
+    // |d| = m * 2^(e - 1075), m the 53-bit significand (e = 0 has none: too
+    // small to matter here); in units of 2^-149: m >> (926 - e), 30..53 bits
+    unsigned long long const m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    uint32_t const sh = 926u - e;
+    unsigned long long const q = m >> sh, rest = m & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    r = (uint32_t)q + (uint32_t)(rest > half || (rest == half && (q & 1ull)));
+  }
+  return __uint_as_float(sign | r);
 }
 
 // TMA staging of one tile: rows (which, fl, ia) of the two blocks, the
