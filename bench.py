@@ -271,6 +271,34 @@ def main():
             k += len(xs)
         return k
 
+    # FP32 tile copies of the blocks, made once per block (as the driver
+    # does when a solved block enters its cache): a step converts its new
+    # source's block inside the timed region; partners were converted when
+    # they were new
+    blocks32 = {}
+
+    def block32(p, make=True):
+        site = schedule.mod_pos(p, LATTICE)
+        if site not in blocks32:
+            blocks32[site] = torch.empty(c.f32_block_length, dtype=torch.float32, device="cuda")
+            if make:
+                c.f32_tile_copy(block(p), blocks32[site])
+        return blocks32[site]
+
+    def run_batched32(steps, out):
+        """The FP32-copy path: per step, convert the new block, then one
+        batched call over the FP32 copies."""
+        k = 0
+        for st in steps:
+            p, qs = st
+            y32 = block32(p, make=False)
+            c.f32_tile_copy(block(p), y32)
+            pr = pairs_of(st)
+            c.kernel_sums_batched_f32(y32, [block32(q) for q, _, _, _ in pr], [g for _, _, g, _ in pr],
+                                      [v for _, _, _, v in pr], xu, out[k:k + len(pr)])
+            k += len(pr)
+        return k
+
     def run_pairs(steps, prec, out):
         """The per-pair API, one call per pair (the reference driver's loop)."""
         k = 0
@@ -296,37 +324,50 @@ def main():
             ms = float(t.item())
         return n, ms
 
-    def graph_timed(prec):
-        """Record the timed sources' batched calls as one CUDA graph and time
-        one replay (all K steps)."""
+    def graph_timed():
+        """Record the timed sources' work (conversion of each new block and
+        one batched call) as one CUDA graph and time one replay (all K steps)."""
         c.graph_begin()
-        run_batched(timed, prec, res)
+        run_batched32(timed, res)
         graph = c.graph_end()
         clocks = ClockSampler(local_rank)
         n, ms = timeit(lambda: (graph.launch(stream), n_timed_pairs)[1])
         graph.close()
         return n, ms, clocks.stop()
 
-    # ---- headline: batched per new source, FP32 products on the tensor
-    #      cores, FP64 sums, the exact QED weight (FP32 quadrature, FP64 near
+    # ---- headline: batched per new source on FP32 tile copies (one
+    #      conversion per new block), FP32 products (pass 2 on the tensor
+    #      cores), FP64 sums, the exact QED weight (FP32 quadrature, FP64 near
     #      the origin), one CUDA graph for the timed sources, autotuned -------
     c.set_qed(None)
     c.reserve(16)
-    y0, xs0, gs0, vs0 = step_args(warm[0] if warm else timed[0])
+    with torch.cuda.stream(stream):
+        for p, qs in order:
+            for q in qs:
+                block32(q)  # partners were converted when they entered the cache
+        for p, _ in order:
+            block32(p, make=False)  # the new blocks' copies: buffers now, converted in their steps
+    st0 = warm[0] if warm else timed[0]
+    y32_0 = block32(st0[0])
+    pr0 = pairs_of(st0)
     if args.no_autotune:
-        tune = {"p1_tile": 8, "p2": "tensor-core", "batch_group": 1, "ms": None}
-        c.set_tensor_cores(True)
-        c.set_batch_group(1)
+        tune = {"p1": "two stages, 1 CTA/SM", "p2": "tensor-core", "batch_group": 1, "ms": None}
     else:
-        tune = c.autotune(y0, xs0, gs0, vs0, xu, res[:len(xs0)])
-    run_batched(warm, hg.FP32, res)
+        tune = c.autotune_f32(y32_0, [block32(q) for q, _, _, _ in pr0], [g for _, _, g, _ in pr0],
+                              [v for _, _, _, v in pr0], xu, res[:len(pr0)])
+    run_batched32(warm, res)
     stream.synchronize()
-    n32, ms32, clk = graph_timed(hg.FP32)
+    n32, ms32, clk = graph_timed()
     res_main = res.clone()
 
-    # ---- the same without the graph, and per pair (unbatched) -------------
+    # ---- the same without the graph; the FP64-block batched API; per pair --
     res_b = torch.zeros_like(res)
-    nb_, msb = timeit(run_batched, timed, hg.FP32, res_b)
+    nb_, msb = timeit(run_batched32, timed, res_b)
+    y0, xs0, gs0, vs0 = step_args(warm[0] if warm else timed[0])
+    tune64 = {"no_autotune": True} if args.no_autotune else c.autotune(y0, xs0, gs0, vs0, xu, res[:len(xs0)])
+    res_f64b = torch.zeros_like(res)
+    run_batched(timed[:1], hg.FP32, res_f64b)
+    nfb, msfb = timeit(run_batched, timed, hg.FP32, res_f64b)
     res_p = torch.zeros_like(res)
     run_pairs(timed[:1], hg.FP32, res_p)
     npp, mspp = timeit(run_pairs, timed, hg.FP32, res_p)
@@ -342,9 +383,9 @@ def main():
     train_rep["gain_max_err"] = train_rep["max_rel_err_base"] / max(train_rep["max_rel_err_net"], 1e-300)
     train_rep["gain_rms_err"] = train_rep["rms_rel_err_base"] / max(train_rep["rms_rel_err_net"], 1e-300)
     c.set_qed(sur)
-    run_batched(warm, hg.FP32, res)
+    run_batched32(warm, res)
     c.set_qed(sur)  # fallback counter cleared: count the timed replay only
-    nsur, mssur, _ = graph_timed(hg.FP32)
+    nsur, mssur, _ = graph_timed()
     res_sur = res.clone()
     fallbacks = c.qed_fallbacks()
     c.set_qed(None)
@@ -352,8 +393,8 @@ def main():
     # ---- FP32 products with the FP64 weight everywhere -----------------------
     c.set_qed_fp32(False)
     res32x = torch.zeros_like(res)
-    run_batched(timed[:1], hg.FP32, res32x)
-    n32x, ms32x = timeit(run_batched, timed, hg.FP32, res32x)
+    run_batched32(timed[:1], res32x)
+    n32x, ms32x = timeit(run_batched32, timed, res32x)
     c.set_qed_fp32(True)
 
     # ---- plain FP64, per pair, exact weight (the reference's path) on the
@@ -382,11 +423,12 @@ def main():
     rel, chain_rel, rel_fl = errs(res_main)
     rel_sur, chain_sur, rel_sur_fl = errs(res_sur)
     rel32x, chain32x, rel32x_fl = errs(res32x)
+    relfb, chainfb, _ = errs(res_f64b)
     relp, _, _ = errs(res_p)
 
     # ---- per-kernel durations (CUDA events on the launching stream) --------
     c.set_profiling(True)
-    run_batched(timed[:1], hg.FP32, res_b)
+    run_batched32(timed[:1], res_b)
     stream.synchronize()
     (p1ms, p1n), (p2ms, p2n) = c.kernel_times()
     c.set_profiling(False)
@@ -423,8 +465,12 @@ def main():
     h2d += pinned[site0].numel() * 8
     k = 0
     for i, st in enumerate(timed):
-        y_b, xs, gs, vs = step_args(st)
-        c.kernel_sums_batched(y_b, xs, gs, vs, xu, res[k:k + len(xs)], hg.FP32)
+        pr = pairs_of(st)
+        xs = [block32(q) for q, _, _, _ in pr]
+        y32 = block32(st[0], make=False)
+        c.f32_tile_copy(block(st[0]), y32)  # waits for the staged block
+        c.kernel_sums_batched_f32(y32, xs, [g for _, _, g, _ in pr], [v for _, _, _, v in pr], xu,
+                                  res[k:k + len(xs)])
         if i + 1 < len(timed):
             sn = schedule.mod_pos(timed[i + 1][0], LATTICE)
             c.stage_async(block(timed[i + 1][0]), pinned[sn], pinned[sn].numel() * 8, after_compute=False)
@@ -450,14 +496,14 @@ def main():
     traffic = load_traffic()
     # pass 1, per launch of g pairs: both FP64 blocks read (y once, each
     # partner once) and their FP32 tile copies written (half the bytes)
-    p1_bytes = sum((1 + gi) for gi in groups) * blk * 1.5 / max(1, p1n)
+    p1_bytes = sum((1 + gi) for gi in groups) * blk * 0.5 / max(1, p1n)  # FP32 copies read
     p1_gbs = p1_bytes / (p1_avg_ms * 1e-3) / 1e9
     # pass 2, per pair: the 128 x 160 x 288 product per 32 sites per flavour
     # (FMA = 2 flops), algorithmic; the tensor cores issue 3x (3xTF32)
     gemm_flop_pair = 2 * 2 * V * 4 * 288 * 160
     p2_tflops = gemm_flop_pair * n_prof / max(1, p2n) / (p2_avg_ms * 1e-3) / 1e12
     p2_bytes = sum((1 + gi) for gi in groups) * blk * 0.5 / max(1, p2n)  # FP32 tile copies read
-    rl_p1 = {"bound": "hbm", "kernel": f"pass 1, p1_kernel<float,2,{tune['p1_tile']}> (batched)",
+    rl_p1 = {"bound": "hbm", "kernel": f"pass 1 on FP32 tile copies, p1f32_kernel ({tune['p1']}, batched)",
              "achieved": round(p1_gbs, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
              "frac": round(p1_gbs / peaks["hbm_gbs"], 5),
              "traffic": (traffic or {}).get("p1_bytes_per_launch"),
@@ -492,6 +538,7 @@ def main():
                                "(window 1 sources)",
                    "lattice": list(LATTICE), "pairs_timed": n32,
                    "path": "batched per source (autotuned), one CUDA graph for the timed sources; "
+                           "blocks as FP32 tile copies (each new block converted once, in its step); "
                            "FP32 products (pass 2 on the tensor cores, 3xTF32), FP64 sums",
                    "qed_weight": "stand-in (KQED unavailable), exact: FP32 quadrature, FP64 within "
                                  "0.1/m_mu of the origin; the learned weight is the 'surrogate' line",
@@ -517,6 +564,11 @@ def main():
                              "max_rel_err_vs_fp64": rel32x, "chain_total_rel_err_vs_fp64": chain32x,
                              "max_rel_err_per_flavour_vs_fp64": rel32x_fl},
         "batched_no_graph": {"value": round(nb_ / (msb * 1e-3), 4), "unit": "pairs/s"},
+        "batched_fp64_blocks": {"value": round(nfb / (msfb * 1e-3), 4), "unit": "pairs/s",
+                                "path": "hlbl_kernel_sums_batched on the FP64 blocks, no graph (pass 1 "
+                                        "converts and writes the FP32 tile copies for every pair)",
+                                "max_rel_err_vs_fp64": relfb, "chain_total_rel_err_vs_fp64": chainfb,
+                                "autotune": tune64},
         "per_pair": {"value": round(npp / (mspp * 1e-3), 4), "unit": "pairs/s", "max_rel_err_vs_fp64": relp},
         "autotune": tune,
         "e2e": {"value": round(pairs_total / e2e_s, 4), "unit": "pairs/s",
@@ -527,7 +579,10 @@ def main():
                       "fp32_fma_peak_tflops": round(fp32_peak, 2),
                       "fma_peak_source": "measured here (FMA-chain kernel, hlbl_measure_fma_peak)"},
         "clocks": clk,
-        "gpu_launches": sum(7 * len([0 for _ in range(0, len(s[1]), tune["batch_group"])]) for s in timed),
+        # per step: the new block's conversion, then per pair group pass 1,
+        # its reduction, the gamma insertion, the B operand, the weights,
+        # pass 2 and its reduction
+        "gpu_launches": sum(1 + 7 * len(range(0, len(s[1]), tune["batch_group"])) for s in timed),
     }
 
     if rank == 0 and not args.no_cpu_baseline:

@@ -67,6 +67,10 @@ def _load() -> C.CDLL:
         "hlbl_ctx_set_batch_group": (C.c_int, [vp, C.c_int]),
         "hlbl_ctx_set_tensor_cores": (C.c_int, [vp, C.c_int]),
         "hlbl_f32_tile_copy": (C.c_int, [vp, vp, vp]),
+        "hlbl_f32_block_length": (C.c_size_t, [vp]),
+        "hlbl_kernel_sums_batched_f32": (C.c_int, [vp, vp, C.c_int, C.POINTER(vp), i4p, i4p, C.c_double, vp]),
+        "hlbl_autotune_f32": (C.c_int, [vp, vp, C.c_int, C.POINTER(vp), i4p, i4p, C.c_double, vp,
+                                        C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]),
         "hlbl_ctx_set_qed_fp32": (C.c_int, [vp, C.c_int, C.c_double]),
         "hlbl_ctx_reserve": (C.c_int, [vp, C.c_int]),
         "hlbl_stage_async": (C.c_int, [vp, vp, vp, C.c_size_t, C.c_int]),

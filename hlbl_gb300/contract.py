@@ -172,6 +172,32 @@ class Contractor:
         (FP64 inside), or FP64 everywhere."""
         check(lib.hlbl_ctx_set_qed_fp32(self._h, 1 if on else 0, float(r64)))
 
+    @property
+    def f32_block_length(self) -> int:
+        """Floats in one FP32 tile copy of a block."""
+        return int(lib.hlbl_f32_block_length(self._h))
+
+    def kernel_sums_batched_f32(self, d_y32, d_x32s, gsxs, yvs, xunit: float, d_out) -> None:
+        """kernel_sums_batched on FP32 tile copies (f32_tile_copy) of the blocks."""
+        n = len(d_x32s)
+        xs = (C.c_void_p * max(1, n))(*[ptr(s) for s in d_x32s])
+        g = (C.c_int * (4 * max(1, n)))(*[int(v) for p in gsxs for v in p])
+        y = (C.c_int * (4 * max(1, n)))(*[int(v) for p in yvs for v in p])
+        check(lib.hlbl_kernel_sums_batched_f32(self._h, ptr(d_y32), n, xs, g, y, C.c_double(xunit),
+                                               ptr(d_out)))
+
+    def autotune_f32(self, d_y32, d_x32s, gsxs, yvs, xunit: float, d_out) -> dict:
+        """Pick the FP32-copy path's pass-1 variant and pair group on this batch."""
+        n = len(d_x32s)
+        xs = (C.c_void_p * n)(*[ptr(s) for s in d_x32s])
+        g = (C.c_int * (4 * n))(*[int(v) for p in gsxs for v in p])
+        y = (C.c_int * (4 * n))(*[int(v) for p in yvs for v in p])
+        v, grp, ms = C.c_int(), C.c_int(), C.c_double()
+        check(lib.hlbl_autotune_f32(self._h, ptr(d_y32), n, xs, g, y, C.c_double(xunit), ptr(d_out),
+                                    C.byref(v), C.byref(grp), C.byref(ms)))
+        return {"p1": ("one stage, 2 CTAs/SM", "two stages, 1 CTA/SM")[v.value], "p2": "tensor-core",
+                "batch_group": grp.value, "ms": ms.value}
+
     def f32_tile_copy(self, d_block, d_out) -> None:
         """The FP32 tile copy of a block (the tensor-core pass 2's input layout)."""
         check(lib.hlbl_f32_tile_copy(self._h, ptr(d_block), ptr(d_out)))

@@ -103,7 +103,7 @@ __global__ void wait_timeout_selftest_kernel(int* err) {
   if (!ok && threadIdx.x == 0) atomicExch(err, kErrWaitTimeout);
 }
 
-// The FP32 tile copy of one block ([f][ia][tile][6][32][4] floats), with the
+// The FP32 tile copy of one block ([f][ia][tile][2][6][16][4] floats), with the
 // conversion pass 1 uses; sites past V in the last tile are left untouched.
 __global__ void f32_tile_copy_kernel(const double* __restrict__ blk, Geometry geo, float* __restrict__ out) {
   long long const n = geo.V * 24 * 6;  // (f, ia, site, c4)
@@ -115,7 +115,7 @@ __global__ void f32_tile_copy_kernel(const double* __restrict__ blk, Geometry ge
     int const row = (int)(i / (6 * geo.V));  // f*12 + ia
     const double* src = blk + ((size_t)row * geo.V + site) * 24 + 4 * c4;
     float4 const v = make_float4(f64_to_f32(src[0]), f64_to_f32(src[1]), f64_to_f32(src[2]), f64_to_f32(src[3]));
-    *reinterpret_cast<float4*>(out + ((size_t)row * nt32 + (site >> 5)) * (32 * 24) + c4 * 128 + (site & 31) * 4) = v;
+    *reinterpret_cast<float4*>(out + ((size_t)row * nt32 + (site >> 5)) * (32 * 24) + f32_tile_off((int)(site & 31), c4)) = v;
   }
 }
 
@@ -217,6 +217,9 @@ struct hlbl_ctx {
   // FP32 two-flavour pass 2 on the tensor cores (p2_tc.cu); off: CUDA cores
   int tc = 1;
   int grid_tc = 0;
+  int grid_p1f[2] = {0, 0};   // pass 1 on FP32 tile copies: 1 stage / 2 stages
+  int p1f_var = 1;
+  int group_f32 = 0;          // pairs per launch on the FP32-copy path (0: kMaxBatch)
   float* d_x32 = nullptr;     // FP32 tile copies: [1 + pair][f32 block] (y first)
   size_t x32_floats = 0;
   float* d_btu = nullptr;     // tensor-core B operand [kMaxBatch][tc_btu_floats_per_pair]
@@ -411,6 +414,38 @@ int run_pass2(hlbl_ctx* c, const Geometry& geo, const double* y, const PairBatch
   return HLBL_OK;
 }
 
+// The FP32-copy path for one pair group: pass 1 on the copies, reduction,
+// gamma insertion, the tensor-core B operand, the weights and the
+// tensor-core pass 2 (b gives outputs and coordinates; tb the copies).
+int run_group_f32(hlbl_ctx* c, const PairBatch& b, const TcBatch& tb, double xunit) {
+  if (c->stage_pending) {
+    cudaError_t e = cudaStreamWaitEvent(c->stream, c->stage_ev, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "wait for staged block");
+    c->stage_pending = false;
+  }
+  Geometry const& geo = c->geo;
+  int const v = c->p1f_var;
+  int const g1 = per_pair_grid(c->grid_p1f[v], b.n, p1f32_tiles(geo.V));
+  prof_begin(c, 0);
+  p1f32_launch(v, g1, b.n, c->stream, tb, geo, c->d_part1, c->d_err);
+  prof_end(c, 0);
+  p1_reduce_kernel<<<dim3((kDzLen + 255) / 256, 2, b.n), 256, 0, c->stream>>>(c->d_part1, g1, 2, c->d_dz,
+                                                                             nullptr, nullptr);
+  g_build_kernel<<<dim3((kGLen / 2 + 255) / 256, 2, b.n), 256, 0, c->stream>>>(c->d_dz, 2, c->d_g);
+  tc_launch_btu(c->d_g, b.n, c->d_btu, c->stream);
+  if (int rc = run_weights(c, geo, b, xunit, HLBL_FP32)) return rc;
+  P2Args a{};
+  a.xunit = xunit;
+  a.f0 = 0;
+  a.w = c->d_w;
+  int const g2 = per_pair_grid(c->grid_tc, b.n, tc_tiles(geo.V));
+  prof_begin(c, 1);
+  tc_launch_p2(g2, b.n, c->stream, tb, geo, a, c->d_btu, c->d_part2, c->d_err);
+  prof_end(c, 1);
+  p2_reduce_kernel<<<b.n, 32, 0, c->stream>>>(c->d_part2, g2, 2, b, 0);
+  return HLBL_OK;
+}
+
 PairBatch one_pair(const double* src, double* out, const int gsx[4], const int yv[4]) {
   PairBatch b{};
   b.n = 1;
@@ -462,11 +497,11 @@ int hlbl_ctx_create(hlbl_ctx** out, const int global[4], const int local[4],
       (rc = P2D2::init(c->nsm, c->grid_p2d2)) || (rc = P2D1::init(c->nsm, c->grid_p2d1)) ||
       (rc = P2F2::init(c->nsm, c->grid_p2f2)) || (rc = P2F1::init(c->nsm, c->grid_p2f1)) ||
       (rc = P1F2s::init(c->nsm, c->grid_p1f2s)) || (rc = P2F2s::init(c->nsm, c->grid_p2f2s)) ||
-      (rc = tc_init(c->nsm, c->grid_tc)))
+      (rc = tc_init(c->nsm, c->grid_tc)) || (rc = p1f32_init(c->nsm, c->grid_p1f)))
     return bail(rc);
   c->max_grid = std::max({c->grid_p1d2, c->grid_p1d1, c->grid_p1f2, c->grid_p1f1, c->grid_p2d2,
                           c->grid_p2d1, c->grid_p2f2, c->grid_p2f1, c->grid_p1f2s, c->grid_p2f2s,
-                          c->grid_tc});
+                          c->grid_tc, c->grid_p1f[0], c->grid_p1f[1]});
   e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->stage_ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->compute_ev, cudaEventDisableTiming);
@@ -565,6 +600,80 @@ int hlbl_kernel_sum_async(hlbl_ctx* c, const double* src, const double* y, const
   return check_launch("hlbl_kernel_sum launch");
 }
 
+size_t hlbl_f32_block_length(const hlbl_ctx* c) { return c ? f32_block_floats(c->geo.V) : 0; }
+
+int hlbl_kernel_sums_batched_f32(hlbl_ctx* c, const float* y32, int n, const float* const* x32s,
+                                 const int* gsx, const int* yv, double xunit, double* d_out) {
+  if (!c || !y32 || !x32s || !gsx || !yv || !d_out || n < 0)
+    return fail(HLBL_EINVAL, "hlbl_kernel_sums_batched_f32: bad argument");
+  if (!aligned16(y32)) return fail(HLBL_EINVAL, "hlbl_kernel_sums_batched_f32: copies must be 16-byte aligned");
+  for (int i = 0; i < n; ++i) {
+    if (!x32s[i] || !aligned16(x32s[i]))
+      return fail(HLBL_EINVAL, "hlbl_kernel_sums_batched_f32: copy %d null or not 16-byte aligned", i);
+    for (int r = 0; r < 4; ++r)
+      if (gsx[4 * i + r] < 0 || gsx[4 * i + r] >= c->geo.global[r])
+        return fail(HLBL_EINVAL, "hlbl_kernel_sums_batched_f32: gsx of pair %d outside the lattice", i);
+  }
+  if (long long need = c->geo.V * std::min(std::max(n, 1), kMaxBatch); need > c->w_cap && c->capturing)
+    return fail(HLBL_ESTATE, "QED weight buffer too small during graph capture");
+  int const group = c->group_f32 > 0 ? std::min(c->group_f32, kMaxBatch) : kMaxBatch;
+  for (int i0 = 0; i0 < n; i0 += group) {
+    PairBatch b{};
+    TcBatch tb{};
+    b.n = std::min(group, n - i0);
+    tb.y32 = y32;
+    for (int i = 0; i < b.n; ++i) {
+      b.p[i].out = d_out + 2 * (size_t)(i0 + i);
+      tb.x32[i] = x32s[i0 + i];
+      for (int r = 0; r < 4; ++r) {
+        b.p[i].gsx[r] = tb.gsx[i][r] = gsx[4 * (i0 + i) + r];
+        b.p[i].yv[r] = tb.yv[i][r] = yv[4 * (i0 + i) + r];
+      }
+    }
+    if (int rc = run_group_f32(c, b, tb, xunit)) return rc;
+  }
+  return check_launch("hlbl_kernel_sums_batched_f32 launch");
+}
+
+int hlbl_autotune_f32(hlbl_ctx* c, const float* y32, int n, const float* const* x32s, const int* gsx,
+                      const int* yv, double xunit, double* d_out, int* best_variant, int* best_group,
+                      double* best_ms) {
+  if (!c || n < 1) return fail(HLBL_EINVAL, "hlbl_autotune_f32: bad argument");
+  if (int rc = hlbl_ctx_reserve(c, n)) return rc;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double best = 1e300;
+  int bv = 1, bg = 1;
+  int const groups[] = {1, 2, 4, 8, 16};
+  for (int v = 0; v < 2; ++v)
+    for (int g : groups) {
+      if (g > 1 && g / 2 >= n) continue;
+      c->p1f_var = v;
+      c->group_f32 = g;
+      cudaEventRecord(a, c->stream);
+      int rc = hlbl_kernel_sums_batched_f32(c, y32, n, x32s, gsx, yv, xunit, d_out);
+      cudaEventRecord(b, c->stream);
+      cudaError_t e = cudaEventSynchronize(b);
+      if (rc || e != cudaSuccess) {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        return rc ? rc : cuda_fail(e, "hlbl_autotune_f32");
+      }
+      float ms = 0;
+      cudaEventElapsedTime(&ms, a, b);
+      if (ms < best) { best = ms; bv = v; bg = g; }
+    }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  c->p1f_var = bv;
+  c->group_f32 = bg;
+  if (best_variant) *best_variant = bv;
+  if (best_group) *best_group = bg;
+  if (best_ms) *best_ms = best;
+  return HLBL_OK;
+}
+
 int hlbl_kernel_sums_batched(hlbl_ctx* c, const double* y, int n, const double* const* srcs,
                              const int* gsx, const int* yv, double xunit, int precision,
                              double* d_out) {
@@ -601,6 +710,11 @@ int hlbl_kernel_sums_batched(hlbl_ctx* c, const double* y, int n, const double* 
 int hlbl_f32_tile_copy(hlbl_ctx* c, const double* d_block, float* d_out) {
   if (!c || !d_block || !d_out) return fail(HLBL_EINVAL, "hlbl_f32_tile_copy: null argument");
   if (!aligned16(d_block) || !aligned16(d_out)) return fail(HLBL_EINVAL, "hlbl_f32_tile_copy: pointers must be 16-byte aligned");
+  if (c->stage_pending) {  // a block staged on the side stream must have landed
+    cudaError_t e = cudaStreamWaitEvent(c->stream, c->stage_ev, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "wait for staged block");
+    c->stage_pending = false;
+  }
   f32_tile_copy_kernel<<<c->nsm * 8, 256, 0, c->stream>>>(d_block, c->geo, d_out);
   return check_launch("hlbl_f32_tile_copy launch");
 }

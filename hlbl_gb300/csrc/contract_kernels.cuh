@@ -171,6 +171,12 @@ __device__ __forceinline__ void load_row(const double* __restrict__ p, double r[
   }
 }
 
+// An FP32 tile copy of a block: rows (f, ia) of tiles of 32 sites, a tile's
+// row = [half of the tile][16-byte group c4][site in the half][4] floats, so
+// that a half tile (16 sites) of a row is 1.5 KB contiguous and a tile 3 KB.
+// Offset of (site s of its tile, group c4) within a tile's row:
+__host__ __device__ constexpr int f32_tile_off(int s, int c4) { return (s >> 4) * 384 + c4 * 64 + (s & 15) * 4; }
+
 // Pass 1's FP32 path: convert a landed FP64 stage into the FP32 compute copy
 // and, in the same pass, into the FP32 tile copies (y32 by pair 0's CTAs).
 // One unit = (row, 16-byte group c4, site); consecutive threads take
@@ -196,7 +202,7 @@ __device__ __forceinline__ void convert_and_copy(const double* __restrict__ st, 
       int const ff = which == 0 ? f0 + fl : 1 - f0 - fl;
       long long const v = s0 + si;
       *reinterpret_cast<float4*>(dst + ((size_t)(ff * 12 + ia) * nt32 + (size_t)(v >> 5)) * (32 * 24) +
-                                 c4 * 128 + (v & 31) * 4) = f;
+                                 f32_tile_off((int)(v & 31), c4)) = f;
     }
   }
 }

@@ -1,0 +1,221 @@
+// p1_f32.cu -- pass 1 (ker_dzu_dzsu, cuda_lattice.cu:160-262) of the mixed
+// path on FP32 tile copies of the blocks (the layout of f32_tile_off): the
+// blocks are converted once, when they enter the propagator cache
+// (hlbl_f32_tile_copy), instead of in every pair's pass 1, so pass 1 reads
+// half the bytes and converts nothing.
+//
+// The same arithmetic as p1_kernel<float, 2, TS>: thread (fl, ia, ib) forms
+// per site the eight spin-block products of src[fl][ia] and y[1-fl][ib],
+// X_sigma, and adds them into dzsu[sigma] and, weighted by the zerohalf
+// coordinates, dzu[k]; per-tile FP32 sums go into Kahan FP32 accumulators,
+// converted to FP64 at the end; partials per CTA in p1_kernel's layout.
+// A tile is half of a 32-site tile of the copy (16 sites): one 1.5 KB TMA
+// copy per row (48 rows). ST = 1: one stage per CTA, two CTAs per SM (the
+// other CTA computes while one waits); ST = 2: two stages, the next tile
+// prefetched while this one is computed, one CTA per SM.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "contract_kernels.cuh"
+#include "hlbl_gb300.h"
+#include "hlbl_internal.h"
+#include "p2_tc.h"
+
+namespace hg {
+namespace p1f {
+
+constexpr int kTS = 16;                   // sites per tile (half of a copy tile)
+constexpr int kRows = 48;                 // (x, y) x 2 flavours x 12
+constexpr int kRowFloats = kTS * 24;      // 384: [c4][16][4]
+constexpr uint32_t kRowBytes = kRowFloats * 4;
+// staged rows 16 bytes apart more than their length, so that the rows the
+// threads of one warp read (12 y rows, 3 x rows) start in different banks
+constexpr int kRowStride = kRowFloats + 4;
+constexpr int kThreads = 2 * 144;
+
+template <int ST>
+struct Smem {
+  float stage[ST][kRows][kRowStride];
+  float zh[kTS][4];
+};
+
+template <int ST>
+__global__ void __launch_bounds__(kThreads, ST == 1 ? 2 : 1)
+p1f32_kernel(TcBatch tb, Geometry geo, double* __restrict__ partials, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  Smem<ST>& sm = *reinterpret_cast<Smem<ST>*>(smem_raw);
+  __shared__ __align__(8) uint64_t s_bar[ST];
+  __shared__ int s_fail;
+  int const t = threadIdx.x, pi = blockIdx.y;
+  int const fl = t / 144, ia = (t % 144) / 12, ib = t % 12;
+  const float* __restrict__ x32 = tb.x32[pi];
+  const float* __restrict__ y32 = tb.y32;
+  int const gsx[4] = {tb.gsx[pi][0], tb.gsx[pi][1], tb.gsx[pi][2], tb.gsx[pi][3]};
+  long long const nt32 = (geo.V + 31) / 32;
+  long long const ntiles = (geo.V + kTS - 1) / kTS;
+  // rows: which = 0 x at flavour fl, which = 1 y at flavour 1 - fl
+  auto issue = [&](long long tile, int st) {
+    mbar_arrive_expect_tx(&s_bar[st], kRows * kRowBytes);
+    long long const t32 = tile >> 1, half = tile & 1;
+    for (int row = 0; row < kRows; ++row) {
+      int const which = row / 24, f = (row / 12) % 2, i = row % 12;
+      int const ff = which == 0 ? f : 1 - f;
+      const float* src = (which == 0 ? x32 : y32) + ((size_t)(ff * 12 + i) * nt32 + t32) * kRowF32 + half * kRowFloats;
+      bulk_g2s(sm.stage[st][row], src, kRowBytes, &s_bar[st]);
+    }
+  };
+  if (t == 0) {
+    for (int i = 0; i < ST; ++i) mbar_init(&s_bar[i], 1);
+    fence_mbar_init();
+    s_fail = 0;
+  }
+  __syncthreads();
+
+  KahanF acc_u[6][2], acc_s[4][2];
+  long long tile = blockIdx.x;
+  if (t == 0 && tile < ntiles) issue(tile, 0);
+  int it = 0;
+  for (; tile < ntiles; tile += gridDim.x, ++it) {
+    int const st = ST == 1 ? 0 : (it & 1);
+    uint32_t const parity = ST == 1 ? (uint32_t)(it & 1) : (uint32_t)((it >> 1) & 1);
+    // ST = 2: prefetch the next tile into the other stage (its readers passed
+    // the previous iteration's barrier)
+    if (ST == 2 && t == 0 && tile + gridDim.x < ntiles) {
+      fence_proxy_async_smem();
+      issue(tile + gridDim.x, st ^ 1);
+    }
+    const float* Arow = sm.stage[st][0 * 24 + fl * 12 + ia];
+    const float* Brow = sm.stage[st][1 * 24 + fl * 12 + ib];
+    long long const s0 = tile * kTS;
+    int const nvalid = (int)min((long long)kTS, geo.V - s0);
+    for (int it = t; it < kTS * 4; it += blockDim.x) {
+      int const s = it >> 2, r = it & 3;
+      int rel[4];
+      rel_coords(geo, gsx, min(s0 + s, geo.V - 1), rel);
+      sm.zh[s][r] = (float)coord_map_zerohalf(rel[r], geo.global[r]);
+    }
+    if (!mbar_wait(&s_bar[st], parity)) s_fail = 1;
+    __syncthreads();
+    if (s_fail) break;
+    float tu[6][2], ts[4][2];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) tu[k][0] = tu[k][1] = 0.f;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) ts[s][0] = ts[s][1] = 0.f;
+#pragma unroll 1
+    for (int s = 0; s < nvalid; ++s) {
+      float A[24], B[24];
+#pragma unroll
+      for (int c4 = 0; c4 < 6; ++c4) {
+        float4 const a = *reinterpret_cast<const float4*>(Arow + c4 * 64 + s * 4);
+        float4 const b = *reinterpret_cast<const float4*>(Brow + c4 * 64 + s * 4);
+        A[4 * c4] = a.x; A[4 * c4 + 1] = a.y; A[4 * c4 + 2] = a.z; A[4 * c4 + 3] = a.w;
+        B[4 * c4] = b.x; B[4 * c4 + 1] = b.y; B[4 * c4 + 2] = b.z; B[4 * c4 + 3] = b.w;
+      }
+      // P[s1][s2] = sum_c conj(B[s1][c]) A[s2][c] for s2 = s1^2 and 3-s1
+      float pa[4][2], pb[4][2];
+#pragma unroll
+      for (int s1 = 0; s1 < 4; ++s1) {
+        float ar = 0, ai = 0, br = 0, bi = 0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          float const yr = B[2 * (3 * s1 + c)], yi = B[2 * (3 * s1 + c) + 1];
+          int const sa = 2 * (3 * (s1 ^ 2) + c), sb = 2 * (3 * (3 - s1) + c);
+          ar += yr * A[sa] + yi * A[sa + 1];  ai += yr * A[sa + 1] - yi * A[sa];
+          br += yr * A[sb] + yi * A[sb + 1];  bi += yr * A[sb + 1] - yi * A[sb];
+        }
+        pa[s1][0] = ar; pa[s1][1] = ai; pb[s1][0] = br; pb[s1][1] = bi;
+      }
+      float X[4][2];
+#pragma unroll
+      for (int sg = 0; sg < 4; ++sg) {
+        float xr = 0, xi = 0;
+#pragma unroll
+        for (int s1 = 0; s1 < 4; ++s1) {
+          float const* pp = (sg == 0 || sg == 3) ? pa[s1] : pb[s1];
+          float vr, vi;
+          mul_iph(g5g_ph(sg, s1), pp[0], pp[1], vr, vi);
+          xr += vr; xi += vi;
+        }
+        X[sg][0] = xr; X[sg][1] = xi;
+      }
+#pragma unroll
+      for (int sg = 0; sg < 4; ++sg) { ts[sg][0] += X[sg][0]; ts[sg][1] += X[sg][1]; }
+      const float* zh = sm.zh[s];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        int const r = comb_rho(k), g = comb_sigma(k);
+        tu[k][0] += zh[r] * X[g][0] - zh[g] * X[r][0];
+        tu[k][1] += zh[r] * X[g][1] - zh[g] * X[r][1];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) { acc_u[k][0].add(tu[k][0]); acc_u[k][1].add(tu[k][1]); }
+#pragma unroll
+    for (int s = 0; s < 4; ++s) { acc_s[s][0].add(ts[s][0]); acc_s[s][1].add(ts[s][1]); }
+    __syncthreads();  // the stage and zh are rewritten for the next tile
+    if (ST == 1 && t == 0 && tile + gridDim.x < ntiles) {
+      fence_proxy_async_smem();
+      issue(tile + gridDim.x, 0);
+    }
+  }
+  if (s_fail) {
+    // a wait gave up: report it and let the copy it waited for (the only
+    // one in flight) land before the CTA exits (bounded, as everything else)
+    if (t == 0) {
+      if (err) atomicExch(err, kErrWaitTimeout);
+      int const st = ST == 1 ? 0 : (it & 1);
+      mbar_wait(&s_bar[st], ST == 1 ? (uint32_t)(it & 1) : (uint32_t)((it >> 1) & 1));
+      if (ST == 2 && tile + gridDim.x < ntiles)
+        mbar_wait(&s_bar[st ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
+    }
+    return;
+  }
+  double* out = partials + (((size_t)pi * gridDim.x + blockIdx.x) * 2 + fl) * kDzLen;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    out[((k * 12 + ia) * 12 + ib) * 2] = acc_u[k][0].get();
+    out[((k * 12 + ia) * 12 + ib) * 2 + 1] = acc_u[k][1].get();
+  }
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    out[kDzuLen + ((s * 12 + ia) * 12 + ib) * 2] = acc_s[s][0].get();
+    out[kDzuLen + ((s * 12 + ia) * 12 + ib) * 2 + 1] = acc_s[s][1].get();
+  }
+}
+
+}  // namespace p1f
+
+template <int ST>
+int p1f32_init_t(int nsm, int& grid) {
+  size_t const smem = sizeof(p1f::Smem<ST>);
+  cudaError_t e = cudaFuncSetAttribute(p1f::p1f32_kernel<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(p1f::p1f32_kernel<ST>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return cuda_fail(e, "p1f32 smem attribute");
+  int nb = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, p1f::p1f32_kernel<ST>, p1f::kThreads, smem);
+  if (e != cudaSuccess) return cuda_fail(e, "p1f32 occupancy");
+  if (nb < 1) return fail(HLBL_ECUDA, "p1f32 kernel cannot be resident");
+  grid = nb * nsm;
+  return HLBL_OK;
+}
+
+int p1f32_init(int nsm, int grid[2]) {
+  if (int rc = p1f32_init_t<1>(nsm, grid[0])) return rc;
+  return p1f32_init_t<2>(nsm, grid[1]);
+}
+
+long long p1f32_tiles(long long V) { return (V + p1f::kTS - 1) / p1f::kTS; }
+
+void p1f32_launch(int variant, int grid, int npairs, cudaStream_t st, const TcBatch& tb, const Geometry& geo,
+                  double* partials, int* err) {
+  if (variant == 0)
+    p1f::p1f32_kernel<1><<<dim3(grid, npairs), p1f::kThreads, sizeof(p1f::Smem<1>), st>>>(tb, geo, partials, err);
+  else
+    p1f::p1f32_kernel<2><<<dim3(grid, npairs), p1f::kThreads, sizeof(p1f::Smem<2>), st>>>(tb, geo, partials, err);
+}
+
+}  // namespace hg

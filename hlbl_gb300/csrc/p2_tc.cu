@@ -38,9 +38,9 @@
 //   MMA -> epilogue (acc_full), epilogue -> MMA (folded, dotted).
 //
 // Inputs are the FP32 tile copies pass 1 writes while it converts each
-// block (x32/y32: [f][ia][tile][6][32][4] floats, a site's 24 components as
-// six 16-byte groups, 32 sites per tile), so pass 2 reads half the bytes of
-// the FP64 blocks and converts nothing.
+// block (x32/y32: [f][ia][tile][2][6][16][4] floats, f32_tile_off: a site's
+// 24 components as six 16-byte groups, 32 sites per tile in two halves), so
+// pass 2 reads half the bytes of the FP64 blocks and converts nothing.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -442,21 +442,21 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
         float* Ahi = sm.A[as][0] + j * 16 * 32 + s * 4;
         float* Alo = sm.A[as][1] + j * 16 * 32 + s * 4;
         if (s < nvalid) {
-          const float* Yr = sm.Y[p % kYSlots] + s * 4;
+          const float* Yr = sm.Y[p % kYSlots] + f32_tile_off(s, 0);
           float y[24];
 #pragma unroll
           for (int c4 = 0; c4 < 6; ++c4) {
-            float4 const a = *reinterpret_cast<const float4*>(Yr + c4 * 128);
+            float4 const a = *reinterpret_cast<const float4*>(Yr + c4 * 64);
             y[4 * c4] = a.x; y[4 * c4 + 1] = a.y; y[4 * c4 + 2] = a.z; y[4 * c4 + 3] = a.w;
           }
           float d[4][4];  // [mu][pq0 re, pq0 im, pq1 re, pq1 im]
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
-            const float* Sr = Sb + (q0 + h) * kRowF32 + s * 4;
+            const float* Sr = Sb + (q0 + h) * kRowF32 + f32_tile_off(s, 0);
             float x[24];
 #pragma unroll
             for (int c4 = 0; c4 < 6; ++c4) {
-              float4 const b = *reinterpret_cast<const float4*>(Sr + c4 * 128);
+              float4 const b = *reinterpret_cast<const float4*>(Sr + c4 * 64);
               x[4 * c4] = b.x; x[4 * c4 + 1] = b.y; x[4 * c4 + 2] = b.z; x[4 * c4 + 3] = b.w;
             }
             // O[s1][s2] = sum_c Y[s1][c] conj(S[s2][c]), s2 = s1^2 (a) and 3-s1 (b)

@@ -9,10 +9,11 @@
 
 namespace hg {
 
-// FP32 tile copies of a propagator block, written by pass 1 (FP32 path) and
-// read by the tensor-core pass 2: [f][ia][tile][6][32][4] floats, tiles of
-// 32 sites (the last one padded), a site's 24 sink components as six
-// 16-byte groups.
+// FP32 tile copies of a propagator block, written by pass 1 (FP32 path) or
+// hlbl_f32_tile_copy and read by the tensor-core pass 2 and the FP32-input
+// pass 1: [f][ia][tile][2][6][16][4] floats (f32_tile_off), tiles of 32
+// sites in two halves (the last tile padded), a site's 24 sink components as
+// six 16-byte groups.
 constexpr int kTileSites32 = 32;
 constexpr int kRowF32 = kTileSites32 * 24;
 inline size_t f32_block_floats(long long V) {
@@ -35,5 +36,12 @@ void tc_launch_btu(const double* d_g, int npairs, float* d_btu, cudaStream_t st)
 void tc_launch_p2(int grid, int npairs, cudaStream_t st, const TcBatch& tb, const Geometry& geo,
                   const P2Args& a, const float* d_btu, double* partials, int* err);
 long long tc_tiles(long long V);
+
+// Pass 1 on FP32 tile copies (p1_f32.cu); partials in p1_kernel's layout.
+// variant 0: one stage, two CTAs per SM; 1: two stages, one CTA per SM
+int p1f32_init(int nsm, int grid[2]);
+long long p1f32_tiles(long long V);
+void p1f32_launch(int variant, int grid, int npairs, cudaStream_t st, const TcBatch& tb, const Geometry& geo,
+                  double* partials, int* err);
 
 }  // namespace hg

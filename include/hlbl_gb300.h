@@ -120,12 +120,34 @@ int hlbl_autotune(hlbl_ctx* ctx, const double* d_fwd_y, int n, const double* con
                   int* best_p2, int* best_group, double* best_ms);
 
 /* The FP32 tile copy of a block that pass 1 of the FP32 path writes and the
- * tensor-core pass 2 reads: d_out[f][ia][tile][6][32][4] floats, tiles of 32
- * sites ((V + 31) / 32 of them, the last padded and its pad left untouched),
- * a site's 24 sink components as six groups of 4; each value rounded to
- * nearest even from FP64. Asynchronous on the context's stream. No
- * counterpart in the reference. */
+ * tensor-core pass 2 and hlbl_kernel_sums_batched_f32 read:
+ * d_out[f][ia][tile][half][6][16][4] floats, tiles of 32 sites ((V + 31) / 32
+ * of them, the last padded and its pad left untouched) in two halves of 16, a
+ * site's 24 sink components as six groups of 4; each value rounded to
+ * nearest even from FP64. 2 * 12 * tiles * 768 floats. Asynchronous on the
+ * context's stream. No counterpart in the reference. */
 int hlbl_f32_tile_copy(hlbl_ctx* ctx, const double* d_block, float* d_out);
+
+/* Floats in one FP32 tile copy of a block of the context's lattice. */
+size_t hlbl_f32_block_length(const hlbl_ctx* ctx);
+
+/* hlbl_kernel_sums_batched on FP32 tile copies of the blocks (hlbl_f32_tile_copy,
+ * made once per block when it enters the propagator cache): FP32 products
+ * (pass 1 on the copies, pass 2 on the tensor cores), FP64 sums, the FP32
+ * path's exact QED weight or the surrogate. Pair i = (gsx[i], gsx[i] + yv[i])
+ * with partner copy x32s[i]; sums to d_out[2*i], [2*i+1]. Asynchronous on the
+ * context's stream. No counterpart in the reference (the block format of the
+ * reference's cache is FP64 only). */
+int hlbl_kernel_sums_batched_f32(hlbl_ctx* ctx, const float* d_y32, int n, const float* const* d_x32s,
+                                 const int* gsx, const int* yv, double xunit, double* d_out);
+
+/* Autotuner of the FP32-copy path: pass-1 variant (0: one stage, two CTAs per
+ * SM; 1: two stages, one CTA per SM) and pairs per launch (1, 2, 4, 8, 16),
+ * timed on one batch; keeps the fastest. Blocking. No counterpart in the
+ * reference. */
+int hlbl_autotune_f32(hlbl_ctx* ctx, const float* d_y32, int n, const float* const* d_x32s,
+                      const int* gsx, const int* yv, double xunit, double* d_out, int* best_variant,
+                      int* best_group, double* best_ms);
 
 /* Exact QED weight of the FP32 path: the quadrature in FP32 where
  * min(|x|, |y|) >= r64 (units of 1/m_mu) and in FP64 inside (on = 1, the

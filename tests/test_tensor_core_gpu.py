@@ -98,7 +98,7 @@ def test_f32_tile_copy_rounds_like_ieee_and_lays_out_tiles():
     """The FP64 -> FP32 conversion of pass 1 (integer pipe, round to nearest
     even) against numpy's IEEE conversion, bit for bit, on Gaussian values
     and planted edge cases (ties, zeros, subnormals, overflow, infinities);
-    and the tile layout [f][ia][tile][6][32][4] with a ragged last tile."""
+    and the tile layout [f][ia][tile][half][6][16][4] with a ragged last tile."""
     import hlbl_gb300 as hg
 
     lat = (3, 5, 1, 7)  # V = 105: four tiles of 32, the last one ragged
@@ -114,8 +114,46 @@ def test_f32_tile_copy_rounds_like_ieee_and_lays_out_tiles():
     with hg.Contractor(lat) as c:
         c.f32_tile_copy(dev(blk), out)
         c.check()
-    got = out.cpu().numpy().reshape(2 * 12, nt, 6, 32, 4)
+    got = out.cpu().numpy().reshape(2 * 12, nt, 2, 6, 16, 4)
     want = blk.astype(np.float32).reshape(2 * 12, V, 6, 4)
     for site in range(V):
-        a = got[:, site // 32, :, site % 32, :]
+        a = got[:, site // 32, (site % 32) // 16, :, site % 16, :]
         assert np.array_equal(a.view(np.uint32), want[:, site].view(np.uint32)), site
+
+
+@pytest.mark.parametrize("lat", [(6, 4, 4, 4), (3, 5, 1, 7)])
+def test_f32_copy_path_matches_oracle_and_fp64_input_path(lat):
+    """hlbl_kernel_sums_batched_f32 on FP32 tile copies made once per block
+    (hlbl_f32_tile_copy): within 1e-4 of the oracle and within FP32 accuracy
+    (1e-5 at the pair's scale; pass 1's tiling differs) of the same batch on
+    the FP64 blocks; the autotuner's choice stays within the same bars."""
+    import hlbl_gb300 as hg
+
+    xu = hg.xunit(105.658, 0.1)
+    y = S.gaussian_block(lat, 71)
+    srcs = [S.gaussian_block(lat, 80 + i) for i in range(3)]
+    gsxs = [tuple((i + r) % L for r, L in enumerate(lat)) for i in range(3)]
+    yvs = [(1, 0, -1, 1), (0, 1, 1, -1), (2, -1, 0, 0)]
+    with hg.Contractor(lat) as c:
+        d_y, d_srcs = dev(y), [dev(s) for s in srcs]
+        n32 = c.f32_block_length
+        y32 = torch.empty(n32, dtype=torch.float32, device="cuda")
+        x32 = [torch.empty(n32, dtype=torch.float32, device="cuda") for _ in srcs]
+        c.f32_tile_copy(d_y, y32)
+        for d, o in zip(d_srcs, x32):
+            c.f32_tile_copy(d, o)
+        out = torch.zeros((3, 2), dtype=torch.float64, device="cuda")
+        c.kernel_sums_batched_f32(y32, x32, gsxs, yvs, xu, out)
+        ref = torch.zeros_like(out)
+        c.kernel_sums_batched(d_y, d_srcs, gsxs, yvs, xu, ref, hg.FP32)
+        tuned = torch.zeros_like(out)
+        best = c.autotune_f32(y32, x32, gsxs, yvs, xu, tuned)
+        c.kernel_sums_batched_f32(y32, x32, gsxs, yvs, xu, tuned)
+        c.check()
+        got, r64, tun = out.cpu().numpy(), ref.cpu().numpy(), tuned.cpu().numpy()
+    assert best["batch_group"] in (1, 2, 4, 8, 16)
+    for i in range(3):
+        orc = S.oracle_kernel_sum(srcs[i], y, gsxs[i], yvs[i], xu, lat)
+        assert S.pair_rel_err(got[i], orc) <= TOL32
+        assert S.pair_rel_err(tun[i], orc) <= TOL32
+        assert S.pair_rel_err(got[i], r64[i]) <= 1e-5
