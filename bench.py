@@ -454,32 +454,40 @@ def main():
             h.copy_(block(p))
             pinned[site] = h
     host_out = torch.empty((n_timed_pairs, 2), dtype=torch.float64, pin_memory=True)
+
+    def e2e_pass():
+        h2d = d2h = 0
+        site0 = schedule.mod_pos(timed[0][0], LATTICE)
+        # each source's block has its own device buffer, idle while it is staged
+        c.stage_async(block(timed[0][0]), pinned[site0], pinned[site0].numel() * 8, after_compute=False)
+        h2d += pinned[site0].numel() * 8
+        k = 0
+        for i, st in enumerate(timed):
+            pr = pairs_of(st)
+            xs = [block32(q) for q, _, _, _ in pr]
+            y32 = block32(st[0], make=False)
+            c.f32_tile_copy(block(st[0]), y32)  # waits for the staged block
+            c.kernel_sums_batched_f32(y32, xs, [g for _, _, g, _ in pr], [v for _, _, _, v in pr], xu,
+                                      res[k:k + len(xs)])
+            if i + 1 < len(timed):
+                sn = schedule.mod_pos(timed[i + 1][0], LATTICE)
+                c.stage_async(block(timed[i + 1][0]), pinned[sn], pinned[sn].numel() * 8, after_compute=False)
+                h2d += pinned[sn].numel() * 8
+            with torch.cuda.stream(stream):
+                host_out[k:k + len(xs)].copy_(res[k:k + len(xs)], non_blocking=True)
+            d2h += len(xs) * 16
+            k += len(xs)
+        stream.synchronize()
+        return h2d, d2h
+
+    # one untimed pass first: the first copies from freshly pinned pages and
+    # the first launches of this call sequence are not representative
+    e2e_pass()
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
-    h2d = d2h = 0
-    site0 = schedule.mod_pos(timed[0][0], LATTICE)
-    # each source's block has its own device buffer, idle while it is staged
-    c.stage_async(block(timed[0][0]), pinned[site0], pinned[site0].numel() * 8, after_compute=False)
-    h2d += pinned[site0].numel() * 8
-    k = 0
-    for i, st in enumerate(timed):
-        pr = pairs_of(st)
-        xs = [block32(q) for q, _, _, _ in pr]
-        y32 = block32(st[0], make=False)
-        c.f32_tile_copy(block(st[0]), y32)  # waits for the staged block
-        c.kernel_sums_batched_f32(y32, xs, [g for _, _, g, _ in pr], [v for _, _, _, v in pr], xu,
-                                  res[k:k + len(xs)])
-        if i + 1 < len(timed):
-            sn = schedule.mod_pos(timed[i + 1][0], LATTICE)
-            c.stage_async(block(timed[i + 1][0]), pinned[sn], pinned[sn].numel() * 8, after_compute=False)
-            h2d += pinned[sn].numel() * 8
-        with torch.cuda.stream(stream):
-            host_out[k:k + len(xs)].copy_(res[k:k + len(xs)], non_blocking=True)
-        d2h += len(xs) * 16
-        k += len(xs)
-    stream.synchronize()
+    h2d, d2h = e2e_pass()
     e2e_s = time.perf_counter() - t0
     if dist:
         t = torch.tensor([e2e_s], device="cuda")
