@@ -12,6 +12,17 @@
  *   oracle_kernel_sum    Contractor::kernel_sum, src/contract.cpp:104-114
  *   oracle_fill_*        the block fixtures, src/provider.cpp:25-69
  *
+ * and of the 2+2 pieces (kernels/hlbl_kernels/kernels.cu):
+ *
+ *   oracle_pi            Pi(z)[mu][nu], kernel_pi :241-294
+ *   oracle_p1_2p2        P1 slab sums, kernel_p1 :296-339
+ *   oracle_p234          P2_0, P2_1, P3, P4_0, P4_1 per target,
+ *                        kernel_p20 :374-458, kernel_p21 :461-545,
+ *                        kernel_p3 :548-643, kernel_p4 :646-750
+ *   oracle_pieces_2p2    compute_2p2_gpu :753-870 with the per-target
+ *                        reordering of Contractor::pieces_2p2
+ *                        (src/contract.cpp:116-156)
+ *
  * The loops follow the reference's order of operations per site; loop
  * invariants are hoisted (gamma-rotated spinors are formed once per site
  * instead of once per inner iteration), which changes no value. Sums over
@@ -444,4 +455,168 @@ void oracle_g_dzu_dzsu(const double* fwd_src, const double* fwd_y, int iflavor,
   memset(dzsu, 0, sizeof(double) * 1152);
   oracle_dzu_dzsu(dzu, dzsu, fwd_src, fwd_y, iflavor, pc, gsx, global, local);
   oracle_insert_gammas(dzu, dzsu, g_dzu, g_dzsu);
+}
+
+/* ======================================================================
+ * 2+2 pieces (kernels/hlbl_kernels/kernels.cu), one rank's part.
+ * ==================================================================== */
+
+/* Pi(z)[mu][nu] = Re sum_ia (g_nu g5 w_ia)[ia],
+ *   w_ia[ib] = <d_ib, g5 g_mu u_ia>,  u = fwd[iflavor](z), d = fwd[1-iflavor](z)
+ * (kernel_pi, kernels.cu:241-294). pi[z*16 + mu*4 + nu]. */
+void oracle_pi(const double* fwd, long long V, int iflavor, double* pi) {
+#pragma omp parallel for schedule(static)
+  for (long long ix = 0; ix < V; ++ix) {
+    for (int mu = 0; mu < 4; ++mu)
+      for (int nu = 0; nu < 4; ++nu) {
+        acc_t tr = {0.0, 0.0};
+        for (int ia = 0; ia < 12; ++ia) {
+          const double* u = fwd + ((size_t)(iflavor * 12 + ia) * (size_t)V + (size_t)ix) * 24;
+          double gu[24], w[24], hw[24];
+          apply_gamma(mu, u, gu);
+          times_g5(gu);
+          for (int ib = 0; ib < 12; ++ib) {
+            const double* d = fwd + ((size_t)((1 - iflavor) * 12 + ib) * (size_t)V + (size_t)ix) * 24;
+            acc_t re = {0.0, 0.0}, im = {0.0, 0.0};
+            for (int c = 0; c < 12; ++c) {
+              acc_add(&re, d[2 * c] * gu[2 * c] + d[2 * c + 1] * gu[2 * c + 1]);
+              acc_add(&im, d[2 * c] * gu[2 * c + 1] - d[2 * c + 1] * gu[2 * c]);
+            }
+            w[2 * ib] = acc_get(&re);
+            w[2 * ib + 1] = acc_get(&im);
+          }
+          times_g5(w);
+          apply_gamma(nu, w, hw);
+          acc_add(&tr, hw[2 * ia]);
+        }
+        pi[ix * 16 + mu * 4 + nu] = acc_get(&tr);
+      }
+  }
+}
+
+/* P1[rho][sigma][nu][zeta] += sum over this rank's sites z with
+ * (z_rho + pc_rho L_rho - gsw_rho) mod G_rho = zeta of Pi(z)[sigma][nu]
+ * (kernel_p1, kernels.cu:296-339). p1 is [4][4][4][lmax]. */
+void oracle_p1_2p2(const double* pi, const int global[4], const int local[4], const int pc[4],
+                   const int gsw[4], int lmax, double* p1) {
+  size_t const V = (size_t)local[0] * local[1] * local[2] * local[3];
+  for (int rho = 0; rho < 4; ++rho)
+    for (int zr = 0; zr < local[rho]; ++zr) {
+      acc_t sum[16];
+      memset(sum, 0, sizeof sum);
+      for (size_t ix = 0; ix < V; ++ix) {
+        int coord[4];
+        site_coords(ix, local, coord);
+        if (coord[rho] != zr) continue;
+        for (int c = 0; c < 16; ++c) acc_add(&sum[c], pi[ix * 16 + c]);
+      }
+      int const zeta = oracle_mod_pos(zr + local[rho] * pc[rho] - gsw[rho], global[rho]);
+      for (int c = 0; c < 16; ++c) p1[(rho * 16 + c) * lmax + zeta] += acc_get(&sum[c]);
+    }
+}
+
+/* P2_0, P2_1, P3, P4_0, P4_1 of every target (kernels.cu:374-750), this
+ * rank's part, added into p234[(t*5 + geom)*64 + rho*16 + sigma*4 + nu]:
+ *   y = (target - gsw) mod G, x = (z + pc L - gsw) mod G (per direction),
+ *   all kernel arguments mapped to [-L/2, L/2) and scaled by xunit:
+ *   P2_0[k][nu] = sum K(x, y)[k][mu][nu][lam]         Pi[mu][lam]
+ *   P2_1[k][nu] = sum K(y, x)[k][nu][mu][lam]         Pi[mu][lam]
+ *   P3[k][nu]   = sum K(x - y, -y)[k][mu][lam][nu]    Pi[mu][lam]
+ *   P4_0[k][nu] = sum K(y - x, -x)[k][nu][lam][mu]    Pi[mu][lam]
+ *   P4_1: P4_0's terms times xv[rho] into [rho][sigma], times -xv[sigma]
+ *   into [sigma][rho] (xv = the mapped x, unscaled),
+ * with k the (rho, sigma) pair, rho < sigma; -y and -x are mapped on their
+ * own ((G - y) mod G), as the reference does. */
+void oracle_p234(const double* pi, const int global[4], const int local[4], const int pc[4],
+                 const int gsw[4], const int* targets, int n_y, double xunit, double lambda,
+                 double* p234) {
+  size_t const V = (size_t)local[0] * local[1] * local[2] * local[3];
+  int const nt = n_threads();
+  hlbl_qed_params qp;
+  hlbl_qed_params_init(&qp, lambda);
+  acc_t* part = (acc_t*)calloc((size_t)nt * 5 * 64, sizeof(acc_t));
+  for (int t = 0; t < n_y; ++t) {
+    int y[4];
+    double ym[4], ym_minus[4];
+    for (int r = 0; r < 4; ++r) {
+      y[r] = oracle_mod_pos(targets[4 * t + r] - gsw[r], global[r]);
+      ym[r] = oracle_coord_map(y[r], global[r]) * xunit;
+      ym_minus[r] = oracle_coord_map((global[r] - y[r]) % global[r], global[r]) * xunit;
+    }
+    memset(part, 0, sizeof(acc_t) * (size_t)nt * 5 * 64);
+#pragma omp parallel
+    {
+      acc_t* my = part + (size_t)thread_id() * 5 * 64;
+      double kerv[6][4][4][4];
+#pragma omp for schedule(static)
+      for (long long ix = 0; ix < (long long)V; ++ix) {
+        int coord[4], xv[4];
+        double xm[4], xm_minus[4], xmy[4], ymx[4];
+        site_coords((size_t)ix, local, coord);
+        for (int r = 0; r < 4; ++r) {
+          int const x = oracle_mod_pos(coord[r] + pc[r] * local[r] - gsw[r], global[r]);
+          xv[r] = oracle_coord_map(x, global[r]);
+          xm[r] = xv[r] * xunit;
+          xm_minus[r] = oracle_coord_map((global[r] - x) % global[r], global[r]) * xunit;
+          xmy[r] = oracle_coord_map(oracle_mod_pos(x - y[r], global[r]), global[r]) * xunit;
+          ymx[r] = oracle_coord_map(oracle_mod_pos(y[r] - x, global[r]), global[r]) * xunit;
+        }
+        const double* P = pi + ix * 16;
+        for (int g = 0; g < 4; ++g) {
+          if (g == 0) hlbl_qed_kernel(&qp, xm, ym, kerv);
+          else if (g == 1) hlbl_qed_kernel(&qp, ym, xm, kerv);
+          else if (g == 2) hlbl_qed_kernel(&qp, xmy, ym_minus, kerv);
+          else hlbl_qed_kernel(&qp, ymx, xm_minus, kerv);
+          for (int k = 0; k < 6; ++k) {
+            int const rho = comb[k][0], sigma = comb[k][1];
+            for (int nu = 0; nu < 4; ++nu) {
+              acc_t v = {0.0, 0.0};
+              for (int mu = 0; mu < 4; ++mu)
+                for (int lam = 0; lam < 4; ++lam) {
+                  double const kv = g == 0 ? kerv[k][mu][nu][lam]
+                                  : g == 1 ? kerv[k][nu][mu][lam]
+                                  : g == 2 ? kerv[k][mu][lam][nu]
+                                           : kerv[k][nu][lam][mu];
+                  acc_add(&v, kv * P[mu * 4 + lam]);
+                }
+              double const val = acc_get(&v);
+              acc_add(&my[g * 64 + rho * 16 + sigma * 4 + nu], val);
+              if (g == 3) {
+                acc_add(&my[4 * 64 + rho * 16 + sigma * 4 + nu], xv[rho] * val);
+                acc_add(&my[4 * 64 + sigma * 16 + rho * 4 + nu], -(xv[sigma] * val));
+              }
+            }
+          }
+        }
+      }
+    }
+    for (int i = 0; i < 5 * 64; ++i) {
+      acc_t tot = {0.0, 0.0};
+      for (int th = 0; th < nt; ++th) {
+        acc_add(&tot, part[(size_t)th * 5 * 64 + i].s);
+        acc_add(&tot, part[(size_t)th * 5 * 64 + i].c);
+      }
+      p234[(size_t)t * 5 * 64 + i] += acc_get(&tot);
+    }
+  }
+  free(part);
+}
+
+/* compute_2p2_gpu (kernels.cu:753-870) of one rank, in the per-target
+ * layout of Contractor::pieces_2p2 (contract.cpp:116-156):
+ * p1 [4][4][4][lmax] and p234 [n_y][5][64], both overwritten with this
+ * rank's part (the caller sums over ranks). */
+void oracle_pieces_2p2(const double* fwd, int iflavor, const int gsw[4], const int* targets,
+                       int n_y, double xunit, double lambda, const int global[4],
+                       const int local[4], const int pc[4], double* p1, double* p234) {
+  size_t const V = (size_t)local[0] * local[1] * local[2] * local[3];
+  int lmax = global[0];
+  for (int r = 1; r < 4; ++r) lmax = global[r] > lmax ? global[r] : lmax;
+  double* pi = (double*)malloc(sizeof(double) * 16 * (V ? V : 1));
+  oracle_pi(fwd, (long long)V, iflavor, pi);
+  memset(p1, 0, sizeof(double) * 64 * (size_t)lmax);
+  memset(p234, 0, sizeof(double) * 5 * 64 * (size_t)n_y);
+  oracle_p1_2p2(pi, global, local, pc, gsw, lmax, p1);
+  oracle_p234(pi, global, local, pc, gsw, targets, n_y, xunit, lambda, p234);
+  free(pi);
 }

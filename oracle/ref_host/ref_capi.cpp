@@ -1,8 +1,10 @@
 // ref_capi.cpp -- TEST INFRASTRUCTURE. A C entry layer over the reference's
-// own sources (kernels/cuda_lattice.cu, src/contract.cpp, src/provider.cpp,
-// src/gamma.cpp, src/geometry.cpp, src/schedule.cpp), compiled as a host
+// own sources (kernels/cuda_lattice.cu, kernels/hlbl_kernels/kernels.cu,
+// src/contract.cpp, src/provider.cpp, src/gamma.cpp, src/geometry.cpp,
+// src/schedule.cpp), compiled as a host
 // emulation with the shims in ./shim. It lets the fixture script run the
 // reference's code on small lattices to pin the oracle. Never shipped.
+#include <algorithm>
 #include <cstdint>
 #include <stdexcept>
 #include <vector>
@@ -24,15 +26,6 @@ extern "C" void QED_Mkernel_L2(const double Lambda, const double xv[4], const do
   hlbl_qed_params p = t.p;
   p.lambda = Lambda;
   hlbl_qed_kernel(&p, xv, yv, kerv);
-}
-
-// contract.cpp links compute_2p2_gpu (2+2 pieces, not emulated here)
-__host__ void compute_2p2_gpu(double*, double*, double*, int const, int const[4], const int*,
-                              int const, const double[2], QED_kernel_temps, unsigned const,
-                              int const[4], MPI_Comm, unsigned const, unsigned const,
-                              unsigned const, unsigned const, unsigned const, unsigned const,
-                              unsigned const, unsigned const) {
-  throw std::runtime_error("compute_2p2_gpu is not part of the host emulation");
 }
 
 namespace {
@@ -79,6 +72,46 @@ void ref_4pt(double* ks, const double* g_dzu, const double* g_dzsu, const double
   initialise(&kq);
   cu_4pt_contraction(ks, g_dzu, g_dzsu, src, y, f, coord(pc), coord(gsx), Pair{xunit, 0.0},
                      coord(yv), kq, geom(global), geom(local));
+}
+
+// Contractor::pieces_2p2 on one rank with lattice `local` (= global):
+// p1 [4][4][4][Lmax], p234 [n_y][5][64] (contract.cpp:116-156).
+int ref_pieces_2p2(const int local[4], const double* fwd, const int gsw[4], const int* targets,
+                   int n_y, double xunit, double* p1, double* p234) {
+  try {
+    hlbl::Lattice lat(MPI_COMM_WORLD, hlbl::Vec4{1, 1, 1, 1},
+                      hlbl::Vec4{local[0], local[1], local[2], local[3]});
+    QED_kernel_temps kq;
+    initialise(&kq);
+    std::size_t const n = hlbl::block_length(lat);
+    hlbl::DeviceBuffer<double> d(n);
+    d.copy_from_host(fwd, n);
+    hlbl::Contractor c(lat, kq);
+    std::vector<hlbl::Vec4> t;
+    for (int i = 0; i < n_y; ++i)
+      t.push_back(hlbl::Vec4{targets[4 * i], targets[4 * i + 1], targets[4 * i + 2], targets[4 * i + 3]});
+    auto r = c.pieces_2p2(d.get(), hlbl::Vec4{gsw[0], gsw[1], gsw[2], gsw[3]}, t, xunit);
+    std::copy(r.p1.begin(), r.p1.end(), p1);
+    std::copy(r.p234.begin(), r.p234.end(), p234);
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+// compute_2p2_gpu (kernels.cu:753-870) of one rank at position pc: that
+// rank's partial p1 [4][4][4][Lmax] and p234 [5][n_y][64] (the single-rank
+// MPI shim leaves the all-reduce to the caller).
+void ref_compute_2p2(const double* fwd, int iflavor, const int gsw[4], const int* targets, int n_y,
+                     double xunit, const int pc[4], const int global[4], const int local[4],
+                     double* p1, double* p234) {
+  QED_kernel_temps kq;
+  initialise(&kq);
+  double const xu[2] = {xunit, 0.0};
+  unsigned const vol = (unsigned)(local[0] * local[1] * local[2] * local[3]);
+  compute_2p2_gpu(const_cast<double*>(fwd), p1, p234, iflavor, gsw, targets, n_y, xu, kq, vol, pc,
+                  MPI_COMM_WORLD, local[0], local[1], local[2], local[3], global[0], global[1],
+                  global[2], global[3]);
 }
 
 void ref_fill_random_block(const int local[4], std::uint64_t seed, double* out) {

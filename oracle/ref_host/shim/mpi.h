@@ -2,6 +2,7 @@
  * (oracle/ref_host): one process, Cartesian coordinates all zero, reductions
  * are copies. Test infrastructure only. */
 #pragma once
+#include <cstdlib>
 #include <cstring>
 typedef int MPI_Comm;
 typedef int MPI_Datatype;
@@ -16,6 +17,10 @@ typedef int MPI_Info;
 #define MPI_INFO_NULL 0
 #define MPI_COMM_TYPE_SHARED 0
 #define MPI_THREAD_MULTIPLE 3
+#define MPI_IN_PLACE ((void*)1)
+#define MPI_STATUSES_IGNORE ((void*)0)
+#define MPI_SUCCESS 0
+typedef int MPI_Request;
 inline int MPI_Comm_size(MPI_Comm, int* s) { *s = 1; return 0; }
 inline int MPI_Comm_rank(MPI_Comm, int* r) { *r = 0; return 0; }
 inline int MPI_Cart_create(MPI_Comm, int, const int*, const int*, int, MPI_Comm* c) { *c = 2; return 0; }
@@ -25,7 +30,13 @@ inline int MPI_Comm_dup(MPI_Comm c, MPI_Comm* d) { *d = c; return 0; }
 inline int MPI_Comm_free(MPI_Comm*) { return 0; }
 inline int MPI_Comm_split_type(MPI_Comm c, int, int, MPI_Info, MPI_Comm* d) { *d = c; return 0; }
 inline int MPI_Allreduce(const void* s, void* r, int n, MPI_Datatype t, MPI_Op, MPI_Comm) {
-  std::memmove(r, s, (std::size_t)n * (std::size_t)t);
+  if (s != MPI_IN_PLACE) std::memmove(r, s, (std::size_t)n * (std::size_t)t);
   return 0;
 }
+inline int MPI_Iallreduce(const void* s, void* r, int n, MPI_Datatype t, MPI_Op o, MPI_Comm c, MPI_Request* q) {
+  *q = 0;
+  return MPI_Allreduce(s, r, n, t, o, c);
+}
+inline int MPI_Waitall(int, MPI_Request*, void*) { return 0; }
+inline int MPI_Abort(MPI_Comm, int e) { std::exit(e); }
 inline double MPI_Wtime() { return 0.0; }

@@ -60,6 +60,11 @@ def oracle():
         lib.oracle_get_threads.restype = C.c_int
         lib.oracle_set_compensated.argtypes = [C.c_int]
         lib.oracle_get_compensated.restype = C.c_int
+        lib.oracle_pi.argtypes = [vpt, C.c_longlong, C.c_int, vpt]
+        lib.oracle_p1_2p2.argtypes = [vpt, I4, I4, I4, I4, C.c_int, vpt]
+        lib.oracle_p234.argtypes = [vpt, I4, I4, I4, I4, vpt, C.c_int, dp, dp, vpt]
+        lib.oracle_pieces_2p2.argtypes = [vpt, C.c_int, I4, vpt, C.c_int, dp, dp, I4, I4, I4, vpt,
+                                          vpt]
         _oracle = lib
     return _oracle
 
@@ -110,6 +115,19 @@ def oracle_4pt(g_dzu, g_dzsu, src, y, f, gsx, xunit, yv, lattice, local=None, pc
     return float(oracle().oracle_4pt(vp(g_dzu), vp(g_dzsu), vp(src), vp(y), int(f), i4(pc),
                                      i4(gsx), C.c_double(xunit), i4(yv), C.c_double(lam),
                                      i4(lattice), i4(local)))
+
+
+def oracle_pieces_2p2(fwd, gsw, targets, xunit, lattice, local=None, pc=(0, 0, 0, 0),
+                      iflavor=0, lam=0.4):
+    """The 2+2 pieces of one rank: p1 [4,4,4,Lmax], p234 [n_y,5,64]."""
+    local = lattice if local is None else local
+    lmax = max(lattice)
+    tg = np.ascontiguousarray(np.asarray(targets, dtype=np.int32).reshape(-1, 4))
+    p1 = np.zeros(64 * lmax)
+    p234 = np.zeros(len(tg) * 5 * 64)
+    oracle().oracle_pieces_2p2(vp(fwd), int(iflavor), i4(gsw), vp(tg), len(tg), C.c_double(xunit),
+                               C.c_double(lam), i4(lattice), i4(local), i4(pc), vp(p1), vp(p234))
+    return p1.reshape(4, 4, 4, lmax), p234.reshape(len(tg), 5, 64)
 
 
 def golden() -> dict:
