@@ -90,6 +90,13 @@ def _load() -> C.CDLL:
         "hlbl_ctx_qed_fallbacks": (C.c_int, [vp, C.POINTER(C.c_ulonglong)]),
         "hlbl_ctx_kernel_times": (C.c_int, [vp, dp, C.POINTER(C.c_longlong)]),
         "hlbl_measure_fma_peak": (C.c_int, [C.c_int, C.c_int, dp]),
+        "hlbl_2p2_lmax": (C.c_int, [vp]),
+        "hlbl_2p2_reserve": (C.c_int, [vp]),
+        "hlbl_ctx_set_2p2_r64": (C.c_int, [vp, C.c_double]),
+        "hlbl_pieces_2p2": (C.c_int, [vp, vp, i4p, vp, C.c_int, C.c_double, C.c_int, vp, vp]),
+        "hlbl_pieces_2p2_async": (C.c_int, [vp, vp, i4p, vp, C.c_int, C.c_double, C.c_int, vp, vp]),
+        "hlbl_pieces_2p2_f32": (C.c_int, [vp, vp, i4p, vp, C.c_int, C.c_double, vp, vp]),
+        "hlbl_compute_2p2": (C.c_int, [vp, vp, vp, vp, C.c_int, i4p, vp, C.c_int, C.c_double, C.c_int]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

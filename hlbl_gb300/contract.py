@@ -8,6 +8,9 @@ it owns its work buffers and a CUDA stream.
 from __future__ import annotations
 
 import ctypes as C
+from typing import NamedTuple
+
+import numpy as np
 
 from ._lib import check, i4, lib, ptr
 
@@ -26,6 +29,20 @@ def measure_fma_peak(precision=FP64, device: int = 0) -> float:
     out = C.c_double()
     check(lib.hlbl_measure_fma_peak(int(device), _prec(precision), C.byref(out)))
     return out.value
+
+
+class Pieces2p2(NamedTuple):
+    """The 2+2 pieces of one source (include/hlbl/contract.hpp:27-37)."""
+    p1: np.ndarray    # [4][4][4][lmax]
+    p234: np.ndarray  # [n_y][5][4][4][4]: P2_0, P2_1, P3, P4_0, P4_1
+
+
+def _targets(targets):
+    """(int array [n][4], n) of a target list."""
+    flat = [int(v) for t in targets for v in t]
+    if len(flat) % 4:
+        raise ValueError("targets must be 4-vectors")
+    return (C.c_int * max(4, len(flat)))(*flat), len(flat) // 4
 
 
 def _prec(p) -> int:
@@ -243,10 +260,58 @@ class Contractor:
         check(lib.hlbl_reserve_kernel_memory(self._h, C.byref(n)))
         return int(n.value)
 
-    def pieces_2p2(self, *args, **kwargs):
-        """Contractor::pieces_2p2 (contract.cpp:116-156) is not part of this
-        library: the 2+2 pieces are a different contraction."""
-        raise NotImplementedError("the 2+2 pieces (compute_2p2_gpu) are not implemented here")
+    # -- the 2+2 pieces ----------------------------------------------------------
+    @property
+    def lmax(self) -> int:
+        """The last dimension of P1: the largest global extent."""
+        return int(lib.hlbl_2p2_lmax(self._h))
+
+    def set_2p2_r64(self, r64: float) -> None:
+        """FP32 2+2 path: the FP64 QED weight where an argument is shorter
+        than r64 (units of 1/m_mu); 0, the default: FP32 everywhere."""
+        check(lib.hlbl_ctx_set_2p2_r64(self._h, C.c_double(r64)))
+
+    def reserve_2p2(self) -> None:
+        """Allocate the 2+2 work buffers now (before a graph capture)."""
+        check(lib.hlbl_2p2_reserve(self._h))
+
+    def pieces_2p2(self, d_fwd, gsw, targets, xunit: float, precision=FP64) -> "Pieces2p2":
+        """The 2+2 pieces of the source w = gsw for `targets` (global sites in
+        [0, L)) from the device block of w, flavour 0: Contractor::pieces_2p2
+        (src/contract.cpp:116-156). This rank's part (sum over ranks with
+        more than one). p1 flat [4][4][4][lmax], p234 flat [n_y][5][4][4][4]."""
+        tg, n = _targets(targets)
+        p1 = np.zeros(64 * self.lmax)
+        p234 = np.zeros(n * 5 * 64)
+        check(lib.hlbl_pieces_2p2(self._h, ptr(d_fwd), i4(gsw), tg, n, C.c_double(xunit),
+                                  _prec(precision), p1.ctypes.data_as(C.c_void_p),
+                                  p234.ctypes.data_as(C.c_void_p)))
+        return Pieces2p2(p1, p234)
+
+    def pieces_2p2_async(self, d_fwd, gsw, targets, xunit: float, d_p1, d_p234,
+                         precision=FP64) -> None:
+        """As pieces_2p2, asynchronous, into the device buffers d_p1 and d_p234."""
+        tg, n = _targets(targets)
+        check(lib.hlbl_pieces_2p2_async(self._h, ptr(d_fwd), i4(gsw), tg, n,
+                                        C.c_double(xunit), _prec(precision), ptr(d_p1),
+                                        ptr(d_p234)))
+
+    def pieces_2p2_f32(self, d_x32, gsw, targets, xunit: float, d_p1, d_p234) -> None:
+        """As pieces_2p2_async in FP32, from the block's FP32 tile copy."""
+        tg, n = _targets(targets)
+        check(lib.hlbl_pieces_2p2_f32(self._h, ptr(d_x32), i4(gsw), tg, n, C.c_double(xunit),
+                                      ptr(d_p1), ptr(d_p234)))
+
+    def compute_2p2(self, d_fwd_y, iflavor: int, gsw, gycoords, xunit: float, precision=FP64):
+        """compute_2p2_gpu (kernels/hlbl_kernels/kernels.cu:753-870) without its
+        MPI reduction: (P1 flat [4][4][4][lmax], P234 flat [5][n_y][64])."""
+        tg, n = _targets(gycoords)
+        p1 = np.zeros(64 * self.lmax)
+        p234 = np.zeros(n * 5 * 64)
+        check(lib.hlbl_compute_2p2(self._h, ptr(d_fwd_y), p1.ctypes.data_as(C.c_void_p),
+                                   p234.ctypes.data_as(C.c_void_p), int(iflavor), i4(gsw), tg, n,
+                                   C.c_double(xunit), _prec(precision)))
+        return p1, p234
 
     # -- the QED weight ------------------------------------------------------
     def set_qed(self, surrogate=None, r0: float = -1.0) -> None:

@@ -14,6 +14,7 @@
 #include "hlbl_gb300_rng.h"
 #include "hlbl_internal.h"
 #include "p2_tc.h"
+#include "pieces_2p2.h"
 
 namespace {
 
@@ -248,6 +249,11 @@ struct hlbl_ctx {
   double* d_out = nullptr;    // [2]
   double* h_out = nullptr;    // pinned [2]
   int* d_err = nullptr;       // kernels' error flag (a bounded wait gave up)
+  // 2+2 pieces: work buffers, and the device results of the blocking calls
+  hg::P22* p22 = nullptr;
+  double p22_r64 = 0.0;       // FP32 2+2 path: FP64 QED weight within this radius
+  double* d_p22_out = nullptr;
+  size_t p22_out_cap = 0;     // doubles
   // optional per-kernel timing with CUDA events on the launching stream
   bool profiling = false;
   cudaEvent_t ev[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [pass][begin/end]
@@ -548,6 +554,8 @@ void hlbl_ctx_destroy(hlbl_ctx* c) {
   cudaFree(c->d_err);
   cudaFree(c->d_w);
   cudaFree(c->d_fallback);
+  cudaFree(c->d_p22_out);
+  p22_destroy(c->p22);
   if (c->h_out) cudaFreeHost(c->h_out);
   for (auto& pe : c->ev)
     for (auto& e : pe)
@@ -794,6 +802,113 @@ int hlbl_cu_4pt_contraction(hlbl_ctx* c, double* d_ks, const double* d_g_dzu,
   PairBatch const b = one_pair(src, d_ks, gsx, yv);
   if (int rc = run_pass2(c, geo, y, b, xunit, iflavor, 1, HLBL_FP64, 1)) return rc;
   return check_launch("hlbl_cu_4pt_contraction launch");
+}
+
+// ---- 2+2 pieces (pieces_2p2.cu) -----------------------------------------
+
+int hlbl_2p2_lmax(const hlbl_ctx* c) { return c ? p22_lmax(c->geo) : 0; }
+
+int hlbl_ctx_set_2p2_r64(hlbl_ctx* c, double r64) {
+  if (!c) return fail(HLBL_EINVAL, "hlbl_ctx_set_2p2_r64: null context");
+  if (!(r64 >= 0.0)) return fail(HLBL_EINVAL, "hlbl_ctx_set_2p2_r64: r64 = %g", r64);
+  c->p22_r64 = r64;
+  return HLBL_OK;
+}
+
+int hlbl_2p2_reserve(hlbl_ctx* c) {
+  if (!c) return fail(HLBL_EINVAL, "hlbl_2p2_reserve: null context");
+  return p22_reserve(&c->p22, c->geo, c->nsm);
+}
+
+static int p22_args(hlbl_ctx* c, const char* what, const double* fwd, int iflavor, const int gsw[4],
+                    const int* targets, int n_y, int precision) {
+  if (!c || !fwd || !gsw || (n_y > 0 && !targets)) return fail(HLBL_EINVAL, "%s: null argument", what);
+  if (!aligned16(fwd)) return fail(HLBL_EINVAL, "%s: block must be 16-byte aligned", what);
+  if (iflavor != 0 && iflavor != 1) return fail(HLBL_EINVAL, "%s: iflavor must be 0 or 1", what);
+  if (n_y < 0) return fail(HLBL_EINVAL, "%s: n_y = %d", what, n_y);
+  if (precision != HLBL_FP64 && precision != HLBL_FP32) return fail(HLBL_EINVAL, "%s: bad precision %d", what, precision);
+  for (int r = 0; r < 4; ++r)
+    if (gsw[r] < 0 || gsw[r] >= c->geo.global[r])
+      return fail(HLBL_EINVAL, "%s: gsw[%d] = %d outside [0, %d)", what, r, gsw[r], c->geo.global[r]);
+  for (int t = 0; t < n_y; ++t)
+    for (int r = 0; r < 4; ++r)
+      if (targets[4 * t + r] < 0 || targets[4 * t + r] >= c->geo.global[r])
+        return fail(HLBL_EINVAL, "%s: target %d coordinate %d = %d outside [0, %d)", what, t, r,
+                    targets[4 * t + r], c->geo.global[r]);
+  return HLBL_OK;
+}
+
+static int p22_launch(hlbl_ctx* c, const double* fwd, int iflavor, const int gsw[4], const int* targets,
+                      int n_y, double xunit, int precision, double* d_p1, double* d_p234, int raw,
+                      const float* x32 = nullptr) {
+  P22Request rq{};
+  rq.fwd = fwd;
+  rq.x32 = x32;
+  rq.iflavor = iflavor;
+  for (int r = 0; r < 4; ++r) rq.gsw[r] = gsw[r];
+  rq.targets = targets;
+  rq.n_y = n_y;
+  rq.xunit = xunit;
+  rq.precision = precision;
+  rq.r64 = c->p22_r64;
+  rq.d_p1 = d_p1;
+  rq.d_p234 = d_p234;
+  rq.raw_layout = raw;
+  if (int rc = p22_run(&c->p22, c->stream, c->geo, c->qp, c->nsm, c->capturing, rq)) return rc;
+  return check_launch("2+2 launch");
+}
+
+int hlbl_pieces_2p2_async(hlbl_ctx* c, const double* d_fwd, const int gsw[4], const int* targets, int n_y,
+                          double xunit, int precision, double* d_p1, double* d_p234) {
+  if (int rc = p22_args(c, "hlbl_pieces_2p2_async", d_fwd, 0, gsw, targets, n_y, precision)) return rc;
+  if (!d_p1 || (n_y > 0 && !d_p234)) return fail(HLBL_EINVAL, "hlbl_pieces_2p2_async: null output");
+  return p22_launch(c, d_fwd, 0, gsw, targets, n_y, xunit, precision, d_p1, d_p234, 0);
+}
+
+int hlbl_pieces_2p2_f32(hlbl_ctx* c, const float* d_x32, const int gsw[4], const int* targets, int n_y,
+                        double xunit, double* d_p1, double* d_p234) {
+  // the argument checks of the FP64-block call, on the copy's address
+  if (int rc = p22_args(c, "hlbl_pieces_2p2_f32", reinterpret_cast<const double*>(d_x32), 0, gsw, targets, n_y,
+                        HLBL_FP32))
+    return rc;
+  if (!d_p1 || (n_y > 0 && !d_p234)) return fail(HLBL_EINVAL, "hlbl_pieces_2p2_f32: null output");
+  return p22_launch(c, nullptr, 0, gsw, targets, n_y, xunit, HLBL_FP32, d_p1, d_p234, 0, d_x32);
+}
+
+// the blocking calls: results on the device, then copied to the host arrays
+static int p22_blocking(hlbl_ctx* c, const double* fwd, int iflavor, const int gsw[4], const int* targets,
+                        int n_y, double xunit, int precision, double* p1, double* p234, int raw) {
+  if (!p1 || (n_y > 0 && !p234)) return fail(HLBL_EINVAL, "2+2: null output");
+  size_t const n1 = (size_t)64 * p22_lmax(c->geo), n234 = (size_t)n_y * 5 * 64;
+  if (c->p22_out_cap < n1 + n234) {
+    cudaFree(c->d_p22_out);
+    c->d_p22_out = nullptr;
+    c->p22_out_cap = 0;
+    cudaError_t e = cudaMalloc(&c->d_p22_out, (n1 + n234) * sizeof(double));
+    if (e != cudaSuccess) return cuda_fail(e, "2+2 results");
+    c->p22_out_cap = n1 + n234;
+  }
+  if (int rc = p22_launch(c, fwd, iflavor, gsw, targets, n_y, xunit, precision, c->d_p22_out,
+                          c->d_p22_out + n1, raw))
+    return rc;
+  cudaError_t e = cudaMemcpyAsync(p1, c->d_p22_out, n1 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess && n234)
+    e = cudaMemcpyAsync(p234, c->d_p22_out + n1, n234 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "2+2 result copy");
+  return hlbl_ctx_check(c);
+}
+
+int hlbl_pieces_2p2(hlbl_ctx* c, const double* d_fwd, const int gsw[4], const int* targets, int n_y,
+                    double xunit, int precision, double* p1, double* p234) {
+  if (int rc = p22_args(c, "hlbl_pieces_2p2", d_fwd, 0, gsw, targets, n_y, precision)) return rc;
+  return p22_blocking(c, d_fwd, 0, gsw, targets, n_y, xunit, precision, p1, p234, 0);
+}
+
+int hlbl_compute_2p2(hlbl_ctx* c, const double* d_fwd_y, double* P1, double* P234, int iflavor,
+                     const int gsw[4], const int* gycoords, int n_y, double xunit, int precision) {
+  if (int rc = p22_args(c, "hlbl_compute_2p2", d_fwd_y, iflavor, gsw, gycoords, n_y, precision)) return rc;
+  return p22_blocking(c, d_fwd_y, iflavor, gsw, gycoords, n_y, xunit, precision, P1, P234, 1);
 }
 
 int hlbl_reserve_kernel_memory(hlbl_ctx* c, size_t* bytes) {

@@ -51,19 +51,6 @@ struct Neu {
   __device__ __forceinline__ double get() const { return s + c; }
 };
 
-// Kahan's compensated FP32 sum (s - c is the sum): the FP32 path's per-thread
-// sums over its tiles, kept off GB300's FP64 pipe (1/64 of the FP32 rate)
-// until the end.
-struct KahanF {
-  float s = 0.f, c = 0.f;
-  __device__ __forceinline__ void add(float v) {
-    float const y = v - c;
-    float const t = s + y;
-    c = (t - s) - y;
-    s = t;
-  }
-  __device__ __forceinline__ double get() const { return (double)s - (double)c; }
-};
 
 // Input staging: FP64 kernels double-buffer the FP64 tile (TMA into one
 // stage while computing on the other); FP32 kernels keep one FP64 stage and
@@ -82,43 +69,6 @@ constexpr size_t stage_bytes() {
              ? sizeof(double) * (size_t)(2 * 2 * NF * 12 * TS * 24)
              : sizeof(double) * (size_t)(2 * NF * 12 * TS * 24) +
                    sizeof(float) * (size_t)(2 * NF * 12 * row_stride<float, TS>());
-}
-
-// FP64 -> FP32, rounded to nearest even, on the integer pipe only (the
-// conversion instruction issues on GB300's FP64 pipe, 1/64 of the FP32
-// rate). Normal range: the exponent rebased, the top 23 of the 52 mantissa
-// bits, plus the increment the 29 dropped bits call for (a carry may run into
-// the exponent, as rounding requires; past the largest float it gives inf).
-// Outside it, also in integers: FP32 subnormals and zero (the 53-bit
-// significand shifted right with the same rounding), overflow to inf, inf and
-// NaN kept.
-__device__ __forceinline__ float f64_to_f32(double d) {
-  unsigned long long const b = (unsigned long long)__double_as_longlong(d);
-  uint32_t const hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
-  uint32_t const sign = hi & 0x80000000u;
-  uint32_t const e = (hi >> 20) & 0x7FFu;
-  if (e - 897u <= 253u) {
-    uint32_t r = ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-    uint32_t const rest = lo & 0x1FFFFFFFu;
-    r += (uint32_t)(rest > 0x10000000u) | ((uint32_t)(rest == 0x10000000u) & (r & 1u));
-    return __uint_as_float(sign | r);
-  }
-  uint32_t r;
-  if (e == 0x7FFu) {
-    r = ((hi & 0xFFFFFu) | lo) ? 0x7FC00000u : 0x7F800000u;  // NaN (quiet) or inf
-  } else if (e > 1150u) {
-    r = 0x7F800000u;  // beyond the float range: inf
-  } else if (e < 873u) {
-    r = 0u;           // below half the smallest subnormal: zero
-  } else {
-    // |d| = m * 2^(e - 1075), m the 53-bit significand (e = 0 has none: too
-    // small to matter here); in units of 2^-149: m >> (926 - e), 30..53 bits
-    unsigned long long const m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    uint32_t const sh = 926u - e;
-    unsigned long long const q = m >> sh, rest = m & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-    r = (uint32_t)q + (uint32_t)(rest > half || (rest == half && (q & 1ull)));
-  }
-  return __uint_as_float(sign | r);
 }
 
 // TMA staging of one tile: rows (which, fl, ia) of the two blocks, the
@@ -171,11 +121,6 @@ __device__ __forceinline__ void load_row(const double* __restrict__ p, double r[
   }
 }
 
-// An FP32 tile copy of a block: rows (f, ia) of tiles of 32 sites, a tile's
-// row = [half of the tile][16-byte group c4][site in the half][4] floats, so
-// that a half tile (16 sites) of a row is 1.5 KB contiguous and a tile 3 KB.
-// Offset of (site s of its tile, group c4) within a tile's row:
-__host__ __device__ constexpr int f32_tile_off(int s, int c4) { return (s >> 4) * 384 + c4 * 64 + (s & 15) * 4; }
 
 // Pass 1's FP32 path: convert a landed FP64 stage into the FP32 compute copy
 // and, in the same pass, into the FP32 tile copies (y32 by pair 0's CTAs).

@@ -216,6 +216,52 @@ int hlbl_cu_dzu_dzsu_noalloc(double* d_dzu, double* d_dzsu, const double* fwd_sr
 int hlbl_insert_gammas(hlbl_ctx* ctx, const double* d_dzu, const double* d_dzsu,
                        double* d_g_dzu, double* d_g_dzsu);
 
+/* ---- 2+2 pieces ----------------------------------------------------------
+ * The 2+2 pieces of the source w = gsw for n_y targets (global sites in
+ * [0, L)), from the device block of w (block_length doubles), this rank's
+ * part (with more than one rank the caller sums over ranks, as
+ * compute_2p2_gpu's MPI_Iallreduce does, kernels/hlbl_kernels/kernels.cu:824-860):
+ *   P1   [4][4][4][Lmax]  P1[rho][sigma][nu][zeta] = sum of Pi(z)[sigma][nu]
+ *                         over the sites with (z - w)_rho mod L_rho = zeta
+ *                         (0 for zeta >= L_rho), Lmax = hlbl_2p2_lmax
+ *   P234 P2_0, P2_1, P3, P4_0, P4_1 [rho][sigma][nu] per target, rho < sigma
+ *                         (P4_1: rho != sigma), zero elsewhere
+ * with Pi(z)[mu][nu] = Re sum_ia (g_nu g5 <d_ib, g5 g_mu u_ia>)[ia] of
+ * u = fwd[iflavor], d = fwd[1 - iflavor] (kernel_pi, kernels.cu:241-294).
+ * precision HLBL_FP64: FP64 throughout; HLBL_FP32: FP32 products and QED
+ * weight (the FP64 weight where a kernel argument is shorter than
+ * hlbl_ctx_set_2p2_r64's radius, by default nowhere), FP64 sums. */
+/* The last dimension of P1: the largest global extent. */
+int hlbl_2p2_lmax(const hlbl_ctx* ctx);
+/* FP32 2+2 path: evaluate the QED weight in FP64 where min(|a|, |b|) of its
+ * two arguments (units of 1/m_mu) is below r64; 0 (the default): nowhere. */
+int hlbl_ctx_set_2p2_r64(hlbl_ctx* ctx, double r64);
+/* Allocate the 2+2 work buffers now, so that later calls allocate nothing
+ * (graph capture needs this). */
+int hlbl_2p2_reserve(hlbl_ctx* ctx);
+/* Contractor::pieces_2p2 (src/contract.cpp:116-156; include/hlbl/contract.hpp:54-56):
+ * flavour 0, P234 per target, p234[n_y][5][64]; host arrays; blocking. */
+int hlbl_pieces_2p2(hlbl_ctx* ctx, const double* d_fwd, const int gsw[4], const int* targets,
+                    int n_y, double xunit, int precision, double* p1, double* p234);
+/* As hlbl_pieces_2p2, asynchronous on the context's stream, device outputs
+ * d_p1 [4][4][4][Lmax] and d_p234 [n_y][5][64]; capturable into a CUDA
+ * graph after hlbl_2p2_reserve. */
+int hlbl_pieces_2p2_async(hlbl_ctx* ctx, const double* d_fwd, const int gsw[4], const int* targets,
+                          int n_y, double xunit, int precision, double* d_p1, double* d_p234);
+/* As hlbl_pieces_2p2_async with precision HLBL_FP32, from the block's FP32
+ * tile copy (hlbl_f32_tile_copy; hlbl_f32_block_length floats, 16-byte
+ * aligned) instead of the FP64 block: where the copy exists already (the
+ * FP32 kernel-sum path makes one per source), Pi reads half the bytes and
+ * converts nothing. */
+int hlbl_pieces_2p2_f32(hlbl_ctx* ctx, const float* d_x32, const int gsw[4], const int* targets,
+                        int n_y, double xunit, double* d_p1, double* d_p234);
+/* compute_2p2_gpu (kernels/hlbl_kernels/kernels.cu:753-870, declared at
+ * kernels.cuh:10-13) without its MPI reduction: host P1 [4][4][4][Lmax] and
+ * P234 in its own layout [5][n_y][64] (geometry first), flavour iflavor,
+ * targets gycoords[n_y][4]; blocking. */
+int hlbl_compute_2p2(hlbl_ctx* ctx, const double* d_fwd_y, double* P1, double* P234, int iflavor,
+                     const int gsw[4], const int* gycoords, int n_y, double xunit, int precision);
+
 /* Warm-launches every kernel variant on a 2^4 lattice and returns the device
  * bytes that took (Contractor::reserve_kernel_memory, contract.cpp:158-197). */
 int hlbl_reserve_kernel_memory(hlbl_ctx* ctx, size_t* bytes);
