@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--train-samples", type=int, default=4 * 1024 * 1024)
     ap.add_argument("--train-steps", type=int, default=12000)
+    ap.add_argument("--only-2p2", action="store_true",
+                    help="time only the 2+2 pieces of one source (profiling runs)")
     ap.add_argument("--lattice", default=None,
                     help="T,LX,LY,LZ of a smaller lattice (profiling runs); default 48,24,24,24")
     args = ap.parse_args()
@@ -216,6 +218,8 @@ def main():
     from hlbl_gb300.contract import measure_fma_peak
 
     torch.cuda.set_device(local_rank)
+    if args.only_2p2:
+        return run_2p2_only(args, hg, torch, rank)
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -480,15 +484,20 @@ def main():
         stream.synchronize()
         return h2d, d2h
 
-    # one untimed pass first: the first copies from freshly pinned pages and
-    # the first launches of this call sequence are not representative
+    # one untimed pass first (the first copies from freshly pinned pages and
+    # the first launches of this call sequence are not representative), then
+    # three timed passes: the host side of the box is shared, so the median
+    # is reported and all three are listed
     e2e_pass()
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    h2d, d2h = e2e_pass()
-    e2e_s = time.perf_counter() - t0
+    e2e_runs = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        h2d, d2h = e2e_pass()
+        e2e_runs.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(e2e_runs)
     if dist:
         t = torch.tensor([e2e_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -581,7 +590,11 @@ def main():
         "autotune": tune,
         "e2e": {"value": round(pairs_total / e2e_s, 4), "unit": "pairs/s",
                 "h2d_bytes_per_step": int(h2d / max(1, len(timed))),
-                "d2h_bytes_per_step": int(d2h / max(1, len(timed)))},
+                "d2h_bytes_per_step": int(d2h / max(1, len(timed))),
+                "passes_pairs_per_s": [round(pairs_total / t, 2) for t in e2e_runs],
+                "how": "median of three passes over the timed steps after one untimed pass; each "
+                       "step stages its new block from pinned host memory on the side stream while "
+                       "the previous step computes"},
         "roofline": dominant,
         "rooflines": {"pass1": rl_p1, "pass2": rl_p2,
                       "fp32_fma_peak_tflops": round(fp32_peak, 2),
@@ -592,6 +605,19 @@ def main():
         # pass 2 and its reduction
         "gpu_launches": sum(1 + 7 * len(range(0, len(s[1]), tune["batch_group"])) for s in timed),
     }
+
+    # ---- the 2+2 pieces of the first timed source (compute_2p2_gpu) ---------
+    if rank == 0:
+        p0 = timed[0][0]
+        gsw = schedule.mod_pos(p0, LATTICE)
+        out["pieces_2p2"] = bench_2p2(c, hg, torch, stream, block(p0), block32(p0), gsw, xu,
+                                      max(3, args.steps))
+        if not args.no_cpu_baseline:
+            sec22, cores22 = cpu_2p2_seconds(block(p0).cpu().numpy(), gsw, xu)
+            out["pieces_2p2"]["cpu_baseline"] = {
+                "value": round(sec22 * 1e3, 1), "unit": "ms per source", "cores": cores22, "kind": "port",
+                "sample": f"the oracle (FP64, OpenMP): Pi and P1 once plus P2_0..P4_1 of one target, "
+                          f"the target part scaled by {N_TARGETS_2P2}"}
 
     if rank == 0 and not args.no_cpu_baseline:
         p, qs = timed[0]
@@ -613,6 +639,122 @@ def main():
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+N_TARGETS_2P2 = 16  # the README's 2+2 timing is quoted per 16 targets
+
+
+def targets_2p2(gsw, n):
+    """n distinct target sites around the source gsw, seeded."""
+    import numpy as np
+
+    rng = np.random.default_rng(2025)
+    out = []
+    while len(out) < n:
+        t = [int(rng.integers(0, L)) for L in LATTICE]
+        if t not in out and t != list(gsw):
+            out.append(t)
+    return out
+
+
+def bench_2p2(c, hg, torch, stream, fwd, x32, gsw, xu, reps):
+    """The 2+2 pieces of one source for N_TARGETS_2P2 targets
+    (compute_2p2_gpu), timed with CUDA events on the context's stream."""
+    import numpy as np
+
+    targets = targets_2p2(gsw, N_TARGETS_2P2)
+    d1 = torch.zeros(64 * c.lmax, dtype=torch.float64, device="cuda")
+    d234 = torch.zeros(N_TARGETS_2P2 * 320, dtype=torch.float64, device="cuda")
+    c.reserve_2p2()
+
+    def timed(fn, n):
+        fn()
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        c.check()
+        return e0.elapsed_time(e1) / n, d1.cpu().numpy().copy(), d234.cpu().numpy().copy()
+
+    ms_copy, p1c, p234c = timed(lambda: c.pieces_2p2_f32(x32, gsw, targets, xu, d1, d234), reps)
+    ms_blk, p1b, p234b = timed(lambda: c.pieces_2p2_async(fwd, gsw, targets, xu, d1, d234, hg.FP32), reps)
+    ms64, p1d, p234d = timed(lambda: c.pieces_2p2_async(fwd, gsw, targets, xu, d1, d234, hg.FP64), 1)
+
+    def row_err(a, b):
+        a, b = a.reshape(-1, 5, 64), b.reshape(-1, 5, 64)
+        return float(max(np.abs(a[t, g] - b[t, g]).max() / np.abs(b[t, g]).max()
+                         for t in range(a.shape[0]) for g in range(5)))
+
+    V = volume(LATTICE)
+    evals = 4 * N_TARGETS_2P2 * V
+    return {"value": round(ms_copy, 3), "unit": "ms per source", "targets": N_TARGETS_2P2,
+            "path": "hlbl_pieces_2p2_f32: Pi from the source's FP32 tile copy, FP32 products and "
+                    "QED weight (stand-in, FP32 quadrature), FP64 sums over CTAs",
+            "qed_evaluations_per_s": round(evals / (ms_copy * 1e-3), 1),
+            "fp32_from_fp64_block_ms": round(ms_blk, 3),
+            "fp64_ms": round(ms64, 3),
+            "speedup_vs_fp64": round(ms64 / ms_copy, 2),
+            "max_row_rel_err_p234_vs_fp64": row_err(p234c, p234d),
+            "max_rel_err_p1_vs_fp64": float(np.abs(p1c - p1d).max() / np.abs(p1d).max()),
+            "fp32_paths_identical": bool(np.array_equal(p234c, p234b) and np.array_equal(p1c, p1b)),
+            "gpu_launches_per_source": 3 + 5 * ((N_TARGETS_2P2 + 31) // 32),
+            "reference_readme": "compute_2p2_gpu 4.6 s per 16 targets, one GH200, 262,144 sites, "
+                                "real KQED (not comparable weight)"}
+
+
+def run_2p2_only(args, hg, torch, rank):
+    """The 2+2 line alone: one source's Gaussian block, its FP32 tile copy,
+    N_TARGETS_2P2 targets (profiling runs)."""
+    from hlbl_gb300 import schedule
+
+    if rank != 0:
+        return 0
+    xu = hg.xunit(MUON_MEV, SPACING_FM)
+    c = hg.Contractor(LATTICE)
+    stream = torch.cuda.Stream()
+    c.set_stream(stream)
+    gsw = schedule.mod_pos((1, 2, 3, 4), LATTICE)
+    blk = torch.empty(c.block_length, dtype=torch.float64, device="cuda")
+    x32 = torch.empty(c.f32_block_length, dtype=torch.float32, device="cuda")
+    c.fill_gaussian_block(blk, hg.Contractor.source_seed(RUN_SEED, gsw))
+    c.f32_tile_copy(blk, x32)
+    r = bench_2p2(c, hg, torch, stream, blk, x32, gsw, xu, max(3, args.steps))
+    r["lattice"] = list(LATTICE)
+    print(json.dumps(r), flush=True)
+    c.close()
+    return 0
+
+
+def cpu_2p2_seconds(fwd_h, gsw, xu):
+    """The oracle's 2+2 (FP64, OpenMP) for one source: Pi + P1 once and P234
+    of one target, scaled to N_TARGETS_2P2 targets."""
+    import ctypes as C
+
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import support as S
+
+    o = S.oracle()
+    V = volume(LATTICE)
+    tg = np.ascontiguousarray(np.asarray(targets_2p2(gsw, 1), dtype=np.int32))
+    pi = np.zeros(V * 16)
+    p1 = np.zeros(64 * max(LATTICE))
+    p234 = np.zeros(320)
+    z = S.i4([0, 0, 0, 0])
+    o.oracle_set_compensated(0)  # the reference's plain loops
+    t0 = time.perf_counter()
+    o.oracle_pi(S.vp(fwd_h), V, 0, S.vp(pi))
+    o.oracle_p1_2p2(S.vp(pi), S.i4(LATTICE), S.i4(LATTICE), z, S.i4(gsw), max(LATTICE), S.vp(p1))
+    t1 = time.perf_counter()
+    o.oracle_p234(S.vp(pi), S.i4(LATTICE), S.i4(LATTICE), z, S.i4(gsw), S.vp(tg), 1, C.c_double(xu),
+                  C.c_double(0.4), S.vp(p234))
+    t2 = time.perf_counter()
+    o.oracle_set_compensated(1)
+    return (t1 - t0) + N_TARGETS_2P2 * (t2 - t1), int(o.oracle_get_threads())
 
 
 def run_reference(args, rank, world):

@@ -6,6 +6,10 @@ their last pair. Two pair loops:
   batched   one kernel_sums_batched per new source (all pairs it closes share
             its block), optionally recorded as one CUDA graph per window.
 
+With `sources_2p2` ({global site: [targets]}), the first solve of each of
+those sites computes its 2+2 pieces from the freshly solved block, before the
+block is stored (driver.cpp:58-96: Contractor.pieces_2p2 in the solve step).
+
 `provider(site, dest)` fills a block for a global site (the reference's
 PropagatorProvider::compute); `contract` is a Contractor (or, in CPU tests,
 any object with the same two methods).
@@ -31,18 +35,34 @@ class PairResult:
 
 
 @dataclass
+class Result2p2:
+    """output.hpp Result2p2: the source w, its targets y and y - w, chain,
+    window, and the pieces (p1 [4][4][4][Lmax], p234 [n_y][5][64])."""
+    w: tuple
+    y: list
+    yv: list
+    chain: int
+    window: int
+    p1: object = None
+    p234: object = None
+
+
+@dataclass
 class RunStats:
     positions_solved: int = 0
     pairs: int = 0
     cache_peak: int = 0
     windows: List[int] = field(default_factory=list)
+    pieces_2p2: int = 0
+    targets_2p2: int = 0
 
 
 def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cache: PropagatorCache,
               chain: int = 0, precision=0, batched: bool = False, graphs: bool = False,
-              out_factory=None):
+              out_factory=None, sources_2p2=None, results_2p2=None):
     """One chain; returns ([PairResult], RunStats). With batched=True,
-    out_factory(n) must return a device buffer of n x 2 doubles."""
+    out_factory(n) must return a device buffer of n x 2 doubles. The 2+2
+    results of `sources_2p2` are appended to `results_2p2` (a list)."""
     pending = {}
     for older, newer, _ in sch.all_pairs(steps):
         pending[older] = pending.get(older, 0) + 1
@@ -51,6 +71,25 @@ def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cach
     wrap = lambda p: sch.mod_pos(p, lattice)  # noqa: E731
     results: List[PairResult] = []
     stats = RunStats()
+    todo_2p2 = {tuple(wrap(k)): list(v) for k, v in (sources_2p2 or {}).items()}
+    if todo_2p2 and results_2p2 is None:
+        raise ValueError("run_chain: sources_2p2 needs a results_2p2 list")
+
+    def solve(window, position):
+        dest = cache.begin_insert(position)
+        site = tuple(wrap(position))
+        provider(site, dest)
+        stats.positions_solved += 1
+        # 2+2 at the site's first solve, from the block just solved
+        targets = todo_2p2.pop(site, None)
+        if targets is not None:
+            pc = contractor.pieces_2p2(dest, site, targets, xunit, precision)
+            results_2p2.append(Result2p2(site, [tuple(t) for t in targets],
+                                         [tuple(sch.site_map_diff(t, site, lattice)) for t in targets],
+                                         chain, window, pc.p1, pc.p234))
+            stats.pieces_2p2 += 1
+            stats.targets_2p2 += len(targets)
+        cache.end_insert(position)
     if batched and cache.residency != "device":
         raise ValueError("the batched loop needs the device cache (every partner resident)")
     for st in steps:
@@ -59,10 +98,7 @@ def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cach
             # the reference's order: each source contracted right after its
             # solve, pair by pair (driver.cpp:104-134); peak 16
             for src in st.sources:
-                dest = cache.begin_insert(src.position)
-                provider(wrap(src.position), dest)
-                stats.positions_solved += 1
-                cache.end_insert(src.position)
+                solve(st.index, src.position)
                 if not src.partners:
                     continue
                 gy = wrap(src.position)
@@ -80,10 +116,7 @@ def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cach
             # 30), then one batched call per new source, optionally recorded
             # as one CUDA graph for the window
             for src in st.sources:
-                dest = cache.begin_insert(src.position)
-                provider(wrap(src.position), dest)
-                stats.positions_solved += 1
-                cache.end_insert(src.position)
+                solve(st.index, src.position)
             calls = []
             for src in st.sources:
                 if not src.partners:

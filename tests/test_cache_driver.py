@@ -33,6 +33,12 @@ class Recorder:
     def kernel_sum(self, d_x, d_y, gx, yv, xunit, precision):
         return float(d_x[0] + 10 * d_y[0]), float(sum(gx) + sum(yv))
 
+    def pieces_2p2(self, d_fwd, gsw, targets, xunit, precision):
+        from hlbl_gb300.contract import Pieces2p2
+
+        # the block it was given, the source and the number of targets
+        return Pieces2p2(np.array([d_fwd[0], sum(gsw)]), np.full(len(targets), float(len(targets))))
+
 
 def provider(site, dest):
     dest[:] = hash(site) % 1000
@@ -54,6 +60,29 @@ def test_driver_loop_matches_schedule_simulation(residency):
     if residency == "host":
         # slot 0 stays staged across a source's partners (propagator_cache.cpp:63-66)
         assert buf.staged < 2 * n_pairs
+
+
+def test_driver_2p2_at_first_solves():
+    """The 2+2 pieces of the listed sources are computed once, at their first
+    solve, from the block just solved (driver.cpp:58-96)."""
+    lat = (6, 6, 6, 6)
+    steps = schedule.build_schedule((1, 1, 1, 1), 1, 2)
+    solved = [tuple(schedule.mod_pos(s.position, lat)) for st in steps for s in st.sources]
+    want = {solved[0]: [(1, 2, 3, 4)], solved[5]: [(0, 0, 0, 0), (5, 5, 5, 5), (1, 1, 1, 1)]}
+    buf = NumpyBuffers()
+    cache = PropagatorCache("device", 4, buf)
+    out = []
+    res, st = run_chain(steps, lat, 0.1, provider, Recorder(), cache, sources_2p2=want,
+                        results_2p2=out)
+    assert st.pieces_2p2 == 2 and st.targets_2p2 == 4
+    assert [r.w for r in out] == [solved[0], solved[5]]
+    for r in out:
+        assert r.p1[0] == hash(r.w) % 1000 and r.p1[1] == sum(r.w)  # the solved block
+        assert r.y == want[r.w] and len(r.p234) == len(r.y)
+        assert r.yv == [tuple(schedule.site_map_diff(t, r.w, lat)) for t in r.y]
+    with pytest.raises(ValueError):
+        run_chain(steps, lat, 0.1, provider, Recorder(), PropagatorCache("device", 4, buf),
+                  sources_2p2=want)
 
 
 def test_cache_errors_as_the_reference():

@@ -1,8 +1,10 @@
 """The driver loop on random fields, as the reference's test_driver_random
 (sanity_check/test_driver_random.cpp:133-234): pair count and cache peak
 from the schedule simulation, device vs host cache giving the same sums, a
-few pairs recomputed directly -- plus the batched loop, with and without a
-CUDA graph per window, against the per-pair loop."""
+few pairs recomputed directly, 2+2 at first solves against direct calls --
+plus the batched loop, with and without a CUDA graph per window, against the
+per-pair loop."""
+import numpy as np
 import pytest
 
 import support as S
@@ -25,16 +27,30 @@ def test_driver_device_host_batched_graphs():
         def provider(site, dest):
             c.fill_random_block(dest, hg.Contractor.source_seed(7, site))
 
-        runs = {}
+        solved = [tuple(schedule.mod_pos(s.position, lat)) for st_ in steps for s in st_.sources]
+        want_2p2 = {solved[1]: [(0, 0, 0, 0), (3, 3, 3, 3)], solved[7]: [(1, 2, 3, 4)]}
+        runs, r22 = {}, {}
         for name, res, batched, graphs in (("device", "device", False, False),
                                            ("host", "host", False, False),
                                            ("batched", "device", True, False),
                                            ("graphs", "device", True, True)):
             cache = PropagatorCache(res, c.block_length, TorchBuffers(c))
+            r22[name] = []
             out = run_chain(steps, lat, xu, provider, c, cache, precision=hg.FP64, batched=batched,
                             graphs=graphs,
-                            out_factory=lambda n: torch.zeros((n, 2), dtype=torch.float64, device="cuda"))
+                            out_factory=lambda n: torch.zeros((n, 2), dtype=torch.float64, device="cuda"),
+                            sources_2p2=want_2p2, results_2p2=r22[name])
             runs[name] = out
+        # 2+2 at the first solves (driver.cpp:58-96) equal direct calls on the
+        # same fields, in every mode (host mode: from the scratch block)
+        for name, rows in r22.items():
+            assert [r.w for r in rows] == [solved[1], solved[7]], name
+            assert runs[name][1].pieces_2p2 == 2 and runs[name][1].targets_2p2 == 3
+            for r in rows:
+                d = torch.empty(c.block_length, dtype=torch.float64, device="cuda")
+                provider(r.w, d)
+                direct = c.pieces_2p2(d, r.w, r.y, xu, hg.FP64)
+                assert np.array_equal(direct.p1, r.p1) and np.array_equal(direct.p234, r.p234)
         dev, st = runs["device"]
         assert st.pairs == n_pairs == len(dev) and st.positions_solved == n_prop
         assert st.cache_peak == peak
