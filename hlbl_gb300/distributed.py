@@ -1,7 +1,9 @@
 """Site sharding over ranks: the reference's domain decomposition
 (src/geometry.cpp:21-36) and its one exchange step, the all-reduce of the
 2,880 pass-1 sums between the passes and of the final sums
-(src/contract.cpp:53-56, :100).
+(src/contract.cpp:53-56, :100). The 2+2 pieces shard the same way: every
+rank computes its sites' part of P1 and P234, and one all-reduce of each
+gives the totals (compute_2p2_gpu's MPI_Iallreduce, kernels.cu:824-860).
 
 Each rank holds its sub-lattice's blocks; ShardedContractor runs pass 1 on
 them, all-reduces the sums over the process group, inserts the gammas, runs
@@ -41,6 +43,14 @@ class GpuBackend:
         return ks
 
 
+    def pieces(self, fwd, gsw, targets, xunit, iflavor):
+        """This rank's P1 [4][4][4][Lmax] and P234 [n_y][5][64] on the device."""
+        p1, p234 = self.c.compute_2p2(fwd, iflavor, gsw, targets, xunit)
+        n = len(targets)
+        p234 = p234.reshape(5, n, 64).transpose(1, 0, 2).copy()
+        return torch.from_numpy(p1).cuda(), torch.from_numpy(p234).cuda()
+
+
 class ShardedContractor:
     """kernel_sum over all ranks of `group`; every rank gets the totals."""
 
@@ -57,3 +67,11 @@ class ShardedContractor:
             dist.all_reduce(part, op=dist.ReduceOp.SUM, group=self.group)
             out.append(float(part.item()))
         return tuple(out)
+
+    def pieces_2p2(self, fwd, gsw, targets, xunit, iflavor=0):
+        """The 2+2 pieces over all ranks of `group`: (P1 [4][4][4][Lmax],
+        P234 [n_y][5][64]) on every rank."""
+        p1, p234 = self.b.pieces(fwd, gsw, targets, xunit, iflavor)
+        dist.all_reduce(p1, op=dist.ReduceOp.SUM, group=self.group)
+        dist.all_reduce(p234, op=dist.ReduceOp.SUM, group=self.group)
+        return p1, p234
