@@ -243,6 +243,7 @@ struct hlbl_ctx {
   // FP32 path, exact weight: FP32 quadrature outside qed_r64 (FP64 inside)
   int qed_fp32 = 1;
   double qed_r64 = 0.1;
+  QedF32 qf{};                // the weight's FP32 quadrature tables (from qp)
   const hlbl_surrogate* sur = nullptr;
   double sur_r0 = 0.0;
   unsigned long long* d_fallback = nullptr;  // rows evaluated exactly inside r0
@@ -378,10 +379,13 @@ int run_weights(hlbl_ctx* c, const Geometry& geo, const PairBatch& b, double xun
                                          c->nsm);
   long long const n = geo.V * 3;
   int const blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)c->nsm * 16 / b.n));
-  if (precision == HLBL_FP32 && c->qed_fp32)
-    qed_weights_fp32_kernel<<<dim3(blocks, b.n), 256, 0, c->stream>>>(geo, wa, c->qed_r64, c->d_w);
-  else
+  if (precision == HLBL_FP32 && c->qed_fp32) {
+    // one thread per site (its three evaluations)
+    int const bs = (int)std::max<long long>(1, std::min<long long>((geo.V + 255) / 256, (long long)c->nsm * 16 / b.n));
+    qed_weights_fp32_kernel<<<dim3(bs, b.n), 256, 0, c->stream>>>(geo, wa, c->qed_r64, c->qf, c->d_w);
+  } else {
     qed_weights_exact_kernel<<<dim3(blocks, b.n), 256, 0, c->stream>>>(geo, wa, c->d_w);
+  }
   return HLBL_OK;
 }
 
@@ -494,6 +498,7 @@ int hlbl_ctx_create(hlbl_ctx** out, const int global[4], const int local[4],
   c->device = device;
   c->geo = geo;
   hlbl_qed_params_init(&c->qp, lambda);
+  qed_f32_tables(c->qp, c->qf);
   auto bail = [&](int rc) { hlbl_ctx_destroy(c); return rc; };
   e = cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) return bail(cuda_fail(e, "SM count"));

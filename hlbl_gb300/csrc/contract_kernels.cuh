@@ -13,6 +13,7 @@
 #include <type_traits>
 
 #include "hlbl_device.cuh"
+#include "qed_f32.cuh"
 
 namespace hg {
 
@@ -535,44 +536,68 @@ static __global__ void qed_weights_exact_kernel(Geometry geo, WArgs args, double
 }
 
 // The mixed-precision path's exact weight: the same 16-node quadrature in
-// FP32 where min(|x|, |y|) >= r64 (every quadrature term is positive, so
-// FP32 keeps ~1e-7 relative accuracy), in FP64 inside that radius (near the
-// origin) -- the FP64 QED evaluation is kept only there.
-static __global__ void qed_weights_fp32_kernel(Geometry geo, WArgs args, double r64, double* __restrict__ w) {
-  long long const n = geo.V * 3;
+// FP32 where min(|a|, |b|) >= r64 (every quadrature term is positive, so
+// FP32 keeps a few 1e-7 relative accuracy; qed_f32.cuh), in FP64 inside that
+// radius (near the origin) -- the FP64 QED evaluation is kept only there.
+// One thread per site: its three evaluations share the site's coordinates
+// (32-bit integer arithmetic, V < 2^31); the invariants are FP64 as in the
+// FP64 weight, the quadrature FP32; the FP64 evaluations near the origin are
+// shared by the warp (one node per lane) instead of run by single lanes.
+static __global__ void qed_weights_fp32_kernel(Geometry geo, WArgs args, double r64, QedF32 qf,
+                                               double* __restrict__ w) {
   int const pi = blockIdx.y;
   int const gsx[4] = {args.batch.p[pi].gsx[0], args.batch.p[pi].gsx[1], args.batch.p[pi].gsx[2], args.batch.p[pi].gsx[3]};
   int const yv[4] = {args.batch.p[pi].yv[0], args.batch.p[pi].yv[1], args.batch.p[pi].yv[2], args.batch.p[pi].yv[3]};
-  w += (size_t)pi * n * HLBL_QED_NW;
-  float const l2 = (float)(args.qp.lambda * args.qp.lambda);
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    double a[4], b[4], X, c, Y, ww[HLBL_QED_NW];
-    qed_args(geo, gsx, yv, args.xunit, i / 3, (int)(i % 3), a, b);
-    hlbl_qed_invariants(a, b, &X, &c, &Y);
-    if (fmin(X, Y) < r64) {
-      hlbl_qed_weights(&args.qp, X, c, Y, ww);
-    } else {
-      float const xf = (float)X, yf = (float)Y, cf = (float)c;
-      float acc[HLBL_QED_NW];
+  w += (size_t)pi * geo.V * 3 * HLBL_QED_NW;
+  unsigned const V = (unsigned)geo.V, stride = gridDim.x * blockDim.x;
+  // every lane runs every iteration (the near-origin evaluations are shared
+  // by the warp); lanes past the end compute on the last site and store nothing
+  for (unsigned base = blockIdx.x * blockDim.x; base < V; base += stride) {
+    unsigned const site = min(base + threadIdx.x, V - 1);
+    bool const valid = base + threadIdx.x < V;
+    unsigned s = site;
+    int c[4];
+    c[3] = (int)(s % (unsigned)geo.local[3]); s /= (unsigned)geo.local[3];
+    c[2] = (int)(s % (unsigned)geo.local[2]); s /= (unsigned)geo.local[2];
+    c[1] = (int)(s % (unsigned)geo.local[1]); s /= (unsigned)geo.local[1];
+    c[0] = (int)s;
+    // the arguments in FP64 (small integers times xunit) and their
+    // invariants |a|, cos(a, b), |b| in FP64, as the FP64 weight has them
+    double xm[4], xmy[4];
 #pragma unroll
-      for (int j = 0; j < HLBL_QED_NW; ++j) acc[j] = 0.f;
-#pragma unroll 4
-      for (int q = 0; q < HLBL_QED_NQ; ++q) {
-        float const u = (float)args.qp.node[q], v = 1.f - u;
-        float r2 = u * u * xf * xf + v * v * yf * yf - 2.f * u * v * xf * yf * cf;
-        r2 = fmaxf(r2, 0.f);
-        float const g = (float)args.qp.weight[q] / (1.f + r2);
-        float const r = sqrtf(r2 + l2);
-        float const h[HLBL_QED_NW] = {1.f, u, v, u * v, u * u, v * v};
-#pragma unroll
-        for (int j = 0; j < HLBL_QED_NW; ++j) acc[j] += g * h[j] * expf(-(float)args.qp.mass[j] * r);
-      }
-#pragma unroll
-      for (int j = 0; j < HLBL_QED_NW; ++j) ww[j] = (double)acc[j];
+    for (int r = 0; r < 4; ++r) {
+      int const G = geo.global[r];
+      int const rel = (c[r] + geo.pc[r] * geo.local[r] - gsx[r] + G) % G;
+      xm[r] = coord_map(rel, G) * args.xunit;
+      xmy[r] = coord_map_diff(rel, yv[r], G) * args.xunit;
     }
+    double ymd[4];
 #pragma unroll
-    for (int j = 0; j < HLBL_QED_NW; ++j) w[i * HLBL_QED_NW + j] = ww[j];
+    for (int r = 0; r < 4; ++r) ymd[r] = coord_map(mod_pos(yv[r], geo.global[r]), geo.global[r]) * args.xunit;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      // e = 0: K(xm, ym), e = 1: K(ym, xm), e = 2: K(xm, x - y)
+      const double* a = e == 1 ? ymd : xm;
+      const double* b = e == 0 ? ymd : (e == 1 ? xm : xmy);
+      double Xd, cd, Yd;
+      hlbl_qed_invariants(a, b, &Xd, &cd, &Yd);
+      bool const near = fmin(Xd, Yd) < r64;
+      double ww[HLBL_QED_NW];
+      {
+        float wf[HLBL_QED_NW];
+        weights_f32<false, false>(qf, (float)Xd, (float)cd, (float)Yd, wf);
+#pragma unroll
+        for (int j = 0; j < HLBL_QED_NW; ++j) ww[j] = (double)wf[j];
+      }
+      // near the origin: the FP64 weight of the FP64 arguments, the warp
+      // sharing each such evaluation (one quadrature node per lane)
+      unsigned const m = __ballot_sync(0xffffffffu, near);
+      if (m) qed_weights_fp64_warp(args.qp, m, Xd, cd, Yd, ww);
+      if (valid) {
+#pragma unroll
+        for (int j = 0; j < HLBL_QED_NW; ++j) w[((size_t)site * 3 + e) * HLBL_QED_NW + j] = ww[j];
+      }
+    }
   }
 }
 

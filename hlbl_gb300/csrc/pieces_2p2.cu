@@ -45,6 +45,7 @@
 #include "hlbl_gb300.h"
 #include "hlbl_internal.h"
 #include "pieces_2p2.h"
+#include "qed_f32.cuh"
 
 namespace hg {
 namespace p22 {
@@ -319,59 +320,6 @@ __device__ __forceinline__ void contract(const T* a, const T* b, const T* w, con
   }
 }
 
-// The hardware approximations (PTX rcp/rsqrt/ex2 .approx.ftz): relative
-// errors of a few 1e-7 on the ranges used here (1 + R^2 >= 1,
-// R^2 + Lambda^2 >= Lambda^2 > 0, exponents <= 0 of moderate size).
-__device__ __forceinline__ float rcp_approx(float x) {
-  float y;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float rsqrt_approx(float x) {
-  float y;
-  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float ex2_approx(float x) {
-  float y;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-
-// The six stand-in weights in FP32: the FP64 definition's quadrature with
-// the per-node factors tabulated in FP32 on the host, exp(-m_j r) as
-// 2^(e2_j r) with e2_j = -m_j log2(e). GEOM (masses in arithmetic
-// progression, m_j = m_0 + j dm, the stand-in's): exp(-m_0 r) g_i/(1+R^2)
-// times powers of exp(-dm r), two operations per weight and node.
-template <bool GEOM>
-__device__ __forceinline__ void weights_f32(const QedF32& q, float X, float c, float Y, float w[6]) {
-  float const X2 = X * X, Y2 = Y * Y, XYc = X * Y * c;
-#pragma unroll
-  for (int j = 0; j < 6; ++j) w[j] = 0.f;
-  // fully unrolled: the node tables (kernel parameters) become immediate
-  // constant operands instead of indexed constant loads
-#pragma unroll
-  for (int i = 0; i < HLBL_QED_NQ; ++i) {
-    float r2 = fmaf(q.uu[i], X2, fmaf(q.vv[i], Y2, q.uv2[i] * XYc));
-    r2 = fmaxf(r2, 0.f);
-    float const g = rcp_approx(1.f + r2);
-    float const v = r2 + q.l2;
-    float const r = v * rsqrt_approx(v);
-    if constexpr (GEOM) {
-      float te = g * ex2_approx(q.e2[0] * r);
-      float const de = ex2_approx(q.de2 * r);
-#pragma unroll
-      for (int j = 0; j < 6; ++j) {
-        w[j] = fmaf(q.wh[i][j], te, w[j]);
-        if (j < 5) te *= de;
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < 6; ++j) w[j] = fmaf(q.wh[i][j] * g, ex2_approx(q.e2[j] * r), w[j]);
-    }
-  }
-}
-
 template <typename T>
 __device__ __forceinline__ void weights(const P234Args& p, const T* a, const T* b, T w[6]) {
   if constexpr (sizeof(T) == 8) {
@@ -636,25 +584,6 @@ void p22_destroy(P22* s) {
   delete s;
 }
 
-void p22_qed_f32(const hlbl_qed_params& qp, QedF32& q) {
-  double const log2e = 1.4426950408889634;  // 1 / ln 2
-  q.l2 = (float)(qp.lambda * qp.lambda);
-  for (int j = 0; j < 6; ++j) q.e2[j] = (float)(-qp.mass[j] * log2e);
-  double const dm = qp.mass[1] - qp.mass[0];
-  q.geometric = 1;
-  for (int j = 2; j < 6; ++j)
-    if (fabs(qp.mass[j] - (qp.mass[0] + j * dm)) > 1e-12 * fabs(qp.mass[j])) q.geometric = 0;
-  q.de2 = (float)(-dm * log2e);
-  for (int i = 0; i < HLBL_QED_NQ; ++i) {
-    double const u = qp.node[i], v = 1.0 - u;
-    q.uu[i] = (float)(u * u);
-    q.vv[i] = (float)(v * v);
-    q.uv2[i] = (float)(-2.0 * u * v);
-    double const h[6] = {1.0, u, v, u * v, u * u, v * v};
-    for (int j = 0; j < 6; ++j) q.wh[i][j] = (float)(qp.weight[i] * h[j]);
-  }
-}
-
 int p22_lmax(const Geometry& geo) {
   int l = geo.global[0];
   for (int r = 1; r < 4; ++r) l = geo.global[r] > l ? geo.global[r] : l;
@@ -711,7 +640,7 @@ int p22_run(P22** st, cudaStream_t stream, const Geometry& geo, const hlbl_qed_p
   args.xunit = rq.xunit;
   args.qp = qp;
   args.r64f = (float)rq.r64;
-  p22_qed_f32(qp, args.qf);
+  qed_f32_tables(qp, args.qf);
   if (rq.precision == HLBL_FP64) launch_all<double>(s, stream, geo, rq, args);
   else launch_all<float>(s, stream, geo, rq, args);
   e = cudaGetLastError();

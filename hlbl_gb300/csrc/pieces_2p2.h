@@ -4,23 +4,12 @@
 #include <cuda_runtime.h>
 
 #include "hlbl_device.cuh"
+#include "qed_f32.cuh"
 
 namespace hg {
 
 // targets per launch of the per-target kernels (more are done in chunks)
 constexpr int kMaxTargets = 32;
-
-// The stand-in QED weight's quadrature tabulated in FP32: per node u_i the
-// factors of R_i^2 = uu X^2 + vv Y^2 + uv2 X Y c and g_i h_j(u_i); the
-// exponents as powers of two, e2_j = -m_j log2(e).
-struct QedF32 {
-  float l2;
-  float e2[HLBL_QED_NW];
-  int geometric;            // m_j = m_0 + j dm for every j
-  float de2;                // -dm log2(e)
-  float uu[HLBL_QED_NQ], vv[HLBL_QED_NQ], uv2[HLBL_QED_NQ];
-  float wh[HLBL_QED_NQ][HLBL_QED_NW];
-};
 
 // Kernel parameters of the per-target kernels.
 struct P234Args {
