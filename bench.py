@@ -9,20 +9,22 @@ hypercube schedule with stride 2, h = (+1,-1,+1,-1), K = 4 (76 propagators,
 sources of window 1 in solve order: up to 8 pairs each, 65 per window).
 
 Printed (one JSON line, rank 0):
-  value      pairs/s of the fastest exact-to-1e-4 path (FP32 per-site
-             products, FP64 sums) over K steps with the blocks resident in
-             HBM (inputs are 3 GB each, far above the 129 MB L2, so no flush
-             is needed between steps);
+  value      pairs/s of the headline path (blocks as FP32 tile copies, FP32
+             per-site products with pass 2 on the tensor cores, FP64 sums,
+             batched per source, one CUDA graph for the timed sources) over K
+             steps with the blocks resident in HBM (inputs are 3 GB each, far
+             above the 129 MB L2, so no flush is needed between steps);
   fp64       pairs/s of the plain FP64 path on the same pairs;
   e2e        the same metric through the C ABI with host buffers: each step
              copies its new block from pinned host memory and reads back its
-             kernel sums;
-  roofline   the pass-2 kernel (the dominant one) against measured HBM
-             bandwidth, plus its FLOP rate against the measured FMA peak;
+             kernel sums (median of five passes);
+  roofline   the dominant kernel (pass 2, against a cuBLAS TF32 GEMM measured
+             in the run; pass 1 against the measured HBM bandwidth beside it);
+  pieces_2p2 the 2+2 pieces of one source for 16 targets (compute_2p2_gpu);
   cpu_baseline  the CPU oracle (the reference's loops restated in C, plain
-             summation, all host threads) on a bounded sample: a slab of
-             time slices of one pair, scaled to the full volume.
+             summation, all host threads) on a bounded sample of one pair.
 
+  python bench.py [--only-2p2] [--lattice T,LX,LY,LZ]   (profiling runs)
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 """
 from __future__ import annotations
