@@ -59,10 +59,12 @@ class RunStats:
 
 def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cache: PropagatorCache,
               chain: int = 0, precision=0, batched: bool = False, graphs: bool = False,
-              out_factory=None, sources_2p2=None, results_2p2=None):
+              out_factory=None, sources_2p2=None, results_2p2=None, at_2p2=None):
     """One chain; returns ([PairResult], RunStats). With batched=True,
-    out_factory(n) must return a device buffer of n x 2 doubles. The 2+2
-    results of `sources_2p2` are appended to `results_2p2` (a list)."""
+    out_factory(n) must return a device buffer of n x 2 doubles. 2+2: either
+    `sources_2p2` ({global site: targets}, at the site's first solve in this
+    chain) or `at_2p2` ({solve position as in the schedule: targets}, a
+    plan over several chains, run_chains); results appended to `results_2p2`."""
     pending = {}
     for older, newer, _ in sch.all_pairs(steps):
         pending[older] = pending.get(older, 0) + 1
@@ -72,8 +74,9 @@ def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cach
     results: List[PairResult] = []
     stats = RunStats()
     todo_2p2 = {tuple(wrap(k)): list(v) for k, v in (sources_2p2 or {}).items()}
-    if todo_2p2 and results_2p2 is None:
-        raise ValueError("run_chain: sources_2p2 needs a results_2p2 list")
+    at = {tuple(k): list(v) for k, v in (at_2p2 or {}).items()}
+    if (todo_2p2 or at) and results_2p2 is None:
+        raise ValueError("run_chain: 2+2 sources need a results_2p2 list")
 
     def solve(window, position):
         dest = cache.begin_insert(position)
@@ -81,7 +84,9 @@ def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cach
         provider(site, dest)
         stats.positions_solved += 1
         # 2+2 at the site's first solve, from the block just solved
-        targets = todo_2p2.pop(site, None)
+        targets = at.pop(tuple(position), None)
+        if targets is None:
+            targets = todo_2p2.pop(site, None)
         if targets is not None:
             pc = contractor.pieces_2p2(dest, site, targets, xunit, precision)
             results_2p2.append(Result2p2(site, [tuple(t) for t in targets],
@@ -151,3 +156,33 @@ def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cach
         raise RuntimeError("run_chain: propagators left in the cache")
     stats.cache_peak = cache.peak
     return results, stats
+
+
+def run_chains(chains, lattice, xunit: float, provider: Callable, contractor, cache: PropagatorCache,
+               precision=0, batched: bool = False, graphs: bool = False, out_factory=None,
+               sources_2p2=None, results_2p2=None):
+    """Several chains over one cache (driver.cpp:169-208): the chains in
+    order, the 2+2 of each source in `sources_2p2` ([(source, targets)]) at
+    its first solve over all chains (schedule.plan_2p2). Returns
+    ([PairResult], RunStats, [warning lines of the plan])."""
+    if not chains:
+        raise RuntimeError("run_chains: no chains")
+    if not xunit > 0:
+        raise RuntimeError("run_chains: xunit (m_mu a) is not set")
+    srcs = [tuple(s) for s, _ in (sources_2p2 or [])]
+    plan = sch.plan_2p2(chains, srcs, lattice)
+    total = RunStats()
+    results: List[PairResult] = []
+    for c, steps in enumerate(chains):
+        at = {pos: list(sources_2p2[i][1]) for pos, i in plan.at[c].items()}
+        res, st = run_chain(steps, lattice, xunit, provider, contractor, cache, chain=c,
+                            precision=precision, batched=batched, graphs=graphs,
+                            out_factory=out_factory, results_2p2=results_2p2, at_2p2=at)
+        results.extend(res)
+        total.positions_solved += st.positions_solved
+        total.pairs += st.pairs
+        total.cache_peak = max(total.cache_peak, st.cache_peak)
+        total.windows.extend(st.windows)
+        total.pieces_2p2 += st.pieces_2p2
+        total.targets_2p2 += st.targets_2p2
+    return results, total, sch.report_2p2(plan, srcs)

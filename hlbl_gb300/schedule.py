@@ -134,3 +134,61 @@ def simulate(steps, interleaved: bool = True):
     if cache:
         raise RuntimeError("simulate: propagators left in the cache after the last pair")
     return n_prop, n_pairs, peak
+
+
+@dataclass
+class Plan2p2:
+    """Which solves are followed by 2+2 (schedule.hpp:93-103): the first solve,
+    over the chains in order (windows, then solve order), of each 2+2 source,
+    sites compared wrapped onto the lattice."""
+    at: List[dict] = field(default_factory=list)           # per chain: position -> source index
+    not_sources: List[Tuple[Vec4, int, int]] = field(default_factory=list)  # (site, chain, window)
+    unsolved: List[int] = field(default_factory=list)     # indices of sources no chain solves
+
+
+def plan_2p2(chains, sources, lattice) -> Plan2p2:
+    """schedule.cpp:284-313."""
+    index = {}
+    for i, s in enumerate(sources):
+        index.setdefault(mod_pos(s, lattice), i)
+    plan = Plan2p2(at=[{} for _ in chains])
+    solved = set()
+    for c, chain in enumerate(chains):
+        for st in chain:
+            for src in st.sources:
+                p = mod_pos(src.position, lattice)
+                if p in solved:
+                    continue
+                solved.add(p)
+                if p in index:
+                    plan.at[c][tuple(src.position)] = index[p]
+                else:
+                    plan.not_sources.append((p, c, st.index))
+    plan.unsolved = [i for i, s in enumerate(sources) if mod_pos(s, lattice) not in solved]
+    return plan
+
+
+def report_2p2(plan: Plan2p2, sources) -> List[str]:
+    """The warnings about a plan (schedule.cpp:315-347), the same lines."""
+    lines: List[str] = []
+    if not sources:
+        return lines
+    max_sites = 10
+    n_not = len(plan.not_sources)
+    if n_not > 0:
+        lines.append(f"WARNING: {n_not} solved source positions are not 2+2 sources (no 2+2 "
+                     "computed for them)")
+        for p, chain, window in plan.not_sources[:max_sites]:
+            lines.append(f"  ({p[0]},{p[1]},{p[2]},{p[3]}) in window {window} of chain {chain}")
+        if n_not > max_sites:
+            lines.append(f"  ... and {n_not - max_sites} more")
+    n_uns = len(plan.unsolved)
+    if n_uns > 0:
+        lines.append(f"WARNING: {n_uns} 2+2 sources are not solved by any chain (no 2+2 "
+                     "computed for them)")
+        for i in plan.unsolved[:max_sites]:
+            p = sources[i]
+            lines.append(f"  ({p[0]},{p[1]},{p[2]},{p[3]})")
+        if n_uns > max_sites:
+            lines.append(f"  ... and {n_uns - max_sites} more")
+    return lines

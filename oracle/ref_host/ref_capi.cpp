@@ -6,6 +6,7 @@
 // reference's code on small lattices to pin the oracle. Never shipped.
 #include <algorithm>
 #include <cstdint>
+#include <string>
 #include <stdexcept>
 #include <vector>
 
@@ -155,6 +156,55 @@ int ref_schedule_pairs(const int h[4], int stride, int n_steps, const int origin
         ++n;
       }
   return n;
+}
+
+// plan_2p2 + report_2p2 over n chains (chain c = build_schedule(h[c], stride,
+// n_steps, origin[c])). Rows: at (chain, position[4], index), not_sources
+// (site[4], chain, window), unsolved (index); the report's lines joined by
+// newlines into `report` (cap bytes). Returns -1 if a buffer is too small.
+int ref_plan_2p2(int n_chains, const int* h, int stride, int n_steps, const int* origin, int n_src,
+                 const int* sources, const int lattice[4], int* at, int max_at, int* n_at, int* not_src,
+                 int max_not, int* n_not, int* unsolved, int max_uns, int* n_uns, char* report,
+                 int cap) {
+  std::vector<hlbl::Schedule> chains;
+  for (int c = 0; c < n_chains; ++c)
+    chains.push_back(hlbl::build_schedule(hlbl::Vec4{h[4 * c], h[4 * c + 1], h[4 * c + 2], h[4 * c + 3]},
+                                          stride, n_steps,
+                                          hlbl::Vec4{origin[4 * c], origin[4 * c + 1], origin[4 * c + 2],
+                                                     origin[4 * c + 3]}));
+  std::vector<hlbl::Vec4> src;
+  for (int i = 0; i < n_src; ++i)
+    src.push_back(hlbl::Vec4{sources[4 * i], sources[4 * i + 1], sources[4 * i + 2], sources[4 * i + 3]});
+  hlbl::Plan2p2 const plan =
+      hlbl::plan_2p2(chains, src, hlbl::Vec4{lattice[0], lattice[1], lattice[2], lattice[3]});
+  int k = 0;
+  for (int c = 0; c < n_chains; ++c)
+    for (const auto& [pos, idx] : plan.at[c]) {
+      if (k >= max_at) return -1;
+      int* r = at + 6 * k++;
+      r[0] = c;
+      for (int i = 0; i < 4; ++i) r[1 + i] = pos[i];
+      r[5] = idx;
+    }
+  *n_at = k;
+  k = 0;
+  for (const auto& [p, c, w] : plan.not_sources) {
+    if (k >= max_not) return -1;
+    int* r = not_src + 6 * k++;
+    for (int i = 0; i < 4; ++i) r[i] = p[i];
+    r[4] = c;
+    r[5] = w;
+  }
+  *n_not = k;
+  if ((int)plan.unsolved.size() > max_uns) return -1;
+  for (std::size_t i = 0; i < plan.unsolved.size(); ++i) unsolved[i] = plan.unsolved[i];
+  *n_uns = (int)plan.unsolved.size();
+  std::string all;
+  for (const auto& line : hlbl::report_2p2(plan, src)) all += line + "\n";
+  if ((int)all.size() + 1 > cap) return -1;
+  std::copy(all.begin(), all.end(), report);
+  report[all.size()] = 0;
+  return 0;
 }
 
 // simulate(kInterleaved): propagators, pairs, peak cache.

@@ -51,7 +51,46 @@ def load_ref():
     lib.ref_compute_2p2.argtypes = [C.c_void_p, C.c_int, I4, C.c_void_p, C.c_int, C.c_double,
                                     I4, I4, I4, C.c_void_p, C.c_void_p]
     lib.ref_fill_random_block.argtypes = [I4, C.c_uint64, C.c_void_p]
+    lib.ref_plan_2p2.restype = C.c_int
+    lib.ref_plan_2p2.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                 I4, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                 C.c_void_p, C.c_int, C.c_void_p, C.c_char_p, C.c_int]
     return lib
+
+
+def sign_vectors():
+    return [[a, b, c, d] for a in (1, -1) for b in (1, -1) for c in (1, -1) for d in (1, -1)]
+
+
+# plan_2p2 cases (schedule.cpp:284-347): (name, lattice, hs, stride, n_steps, origins, sources)
+PLANS = [
+    # all 16 h as 16 chains (the 24^3x48 multi-chain configuration's shape),
+    # sources: solved sites, one given twice, one never solved
+    ("16chains_l6", [6, 6, 6, 6], sign_vectors(), 1, 1, [[0, 0, 0, 0]] * 16,
+     [[1, 1, 1, 1], [0, 0, 0, 0], [5, 5, 5, 5], [7, 1, 1, 1], [3, 3, 3, 3], [2, 0, 1, 5]]),
+    # three chains whose windows wrap onto each other; more than 10 warnings
+    ("3chains_wrap", [8, 4, 4, 4], [[1, 1, 1, 1], [1, -1, 1, -1], [-1, 1, 1, 1]], 2, 2,
+     [[0, 0, 0, 0], [4, 0, 0, 0], [2, 2, 2, 2]],
+     [[2, 2, 2, 2], [6, 2, 2, 2], [0, 1, 0, 1], [4, 0, 0, 0], [12, 4, 4, 4]]),
+]
+
+
+def ref_plan(lib, lat, hs, stride, n_steps, origins, sources):
+    n = len(hs)
+    h = np.ascontiguousarray(np.asarray(hs, dtype=np.int32))
+    o = np.ascontiguousarray(np.asarray(origins, dtype=np.int32))
+    sv = np.ascontiguousarray(np.asarray(sources, dtype=np.int32).reshape(-1, 4))
+    at = np.zeros((4096, 6), dtype=np.int32)
+    ns = np.zeros((4096, 6), dtype=np.int32)
+    un = np.zeros(256, dtype=np.int32)
+    n_at, n_ns, n_un = C.c_int(), C.c_int(), C.c_int()
+    rep = C.create_string_buffer(1 << 16)
+    rc = lib.ref_plan_2p2(n, vp(h), stride, n_steps, vp(o), len(sv), vp(sv), i4(lat), vp(at), 4096,
+                          C.byref(n_at), vp(ns), 4096, C.byref(n_ns), vp(un), 256, C.byref(n_un), rep,
+                          1 << 16)
+    assert rc == 0
+    return {"at": at[:n_at.value].tolist(), "not_sources": ns[:n_ns.value].tolist(),
+            "unsolved": un[:n_un.value].tolist(), "report": rep.value.decode().splitlines()}
 
 
 def volume(v):
@@ -123,6 +162,14 @@ def main() -> int:
                                 "targets": targets, "xunit": xu, "iflavor": 1,
                                 "layout": "p1 [4][4][4][Lmax]; p234_raw [5][n_y][64]",
                                 "ranks": ranks}
+    plans = []
+    for name, lat, hs, stride, n_steps, origins, sources in PLANS:
+        r = ref_plan(lib, lat, hs, stride, n_steps, origins, sources)
+        plans.append({"name": name, "lattice": lat, "h": hs, "stride": stride, "n_steps": n_steps,
+                      "origins": origins, "sources": sources, **r})
+        print("plan", name, len(r["at"]), "at,", len(r["not_sources"]), "not sources,",
+              len(r["unsolved"]), "unsolved", flush=True)
+    out["plan_2p2"] = plans
     with open(OUT, "w") as fh:
         json.dump(out, fh)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")

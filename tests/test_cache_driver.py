@@ -85,6 +85,32 @@ def test_driver_2p2_at_first_solves():
                   sources_2p2=want)
 
 
+def test_run_chains_16_chains_and_2p2_plan():
+    """All 16 h as 16 chains over one cache (driver.cpp:169-208): every
+    chain's pairs, and the 2+2 of each source once, at its first solve over
+    all chains (the plan)."""
+    from hlbl_gb300.driver import run_chains
+
+    lat = (6, 6, 6, 6)
+    chains = [schedule.build_schedule(h, 1, 1) for h in schedule.sign_vectors()]
+    per_chain = [schedule.simulate(c) for c in chains]
+    srcs = [((1, 1, 1, 1), [(0, 0, 0, 0)]), ((5, 5, 5, 5), [(1, 2, 3, 4), (2, 2, 2, 2)]),
+            ((3, 3, 3, 3), [(0, 1, 0, 1)])]
+    out = []
+    cache = PropagatorCache("device", 4, NumpyBuffers())
+    res, st, warn = run_chains(chains, lat, 0.1, provider, Recorder(), cache, sources_2p2=srcs,
+                               results_2p2=out)
+    assert st.pairs == len(res) == sum(p for _, p, _ in per_chain)
+    assert st.positions_solved == sum(n for n, _, _ in per_chain)
+    plan = schedule.plan_2p2(chains, [s for s, _ in srcs], lat)
+    want = sorted(tuple(schedule.mod_pos(pos, lat)) for d in plan.at for pos in d)
+    assert sorted(r.w for r in out) == want and st.pieces_2p2 == len(want)
+    assert len(set(r.w for r in out)) == len(out)  # once per source
+    assert any("not solved by any chain" in w for w in warn)  # (3,3,3,3) is not solved
+    with pytest.raises(RuntimeError):
+        run_chains([], lat, 0.1, provider, Recorder(), cache)
+
+
 def test_cache_errors_as_the_reference():
     cache = PropagatorCache("host", 4, NumpyBuffers(), {(0, 0, 0, 0): 1})
     cache.begin_insert((0, 0, 0, 0))

@@ -82,3 +82,34 @@ def test_driver_device_host_batched_graphs():
             provider(r.x, d_x)
             provider(r.y, d_y)
             assert c.kernel_sum(d_x, d_y, r.x, r.yv, xu, hg.FP64) == r.kernel_sum
+
+
+def test_run_chains_equals_independent_chains():
+    """Two chains over one cache (driver.cpp:169-208) give the pairs and sums
+    of each chain run alone (test_driver_random.cpp's two-chain check), and
+    the 2+2 of a source solved by both chains is computed once."""
+    import hlbl_gb300 as hg
+    from hlbl_gb300 import schedule
+    from hlbl_gb300.cache import PropagatorCache, TorchBuffers
+    from hlbl_gb300.driver import run_chain, run_chains
+
+    lat = (6, 6, 6, 6)
+    xu = hg.xunit(105.6583745, 0.07957)
+    chains = [schedule.build_schedule((1, 1, 1, 1), 1, 1), schedule.build_schedule((-1, 1, -1, 1), 1, 1)]
+    with hg.Contractor(lat) as c:
+        def provider(site, dest):
+            c.fill_random_block(dest, hg.Contractor.source_seed(11, site))
+
+        out22 = []
+        cache = PropagatorCache("device", c.block_length, TorchBuffers(c))
+        res, st, _ = run_chains(chains, lat, xu, provider, c, cache, precision=hg.FP32,
+                                sources_2p2=[((0, 0, 0, 0), [(1, 1, 1, 1)])], results_2p2=out22)
+        alone = []
+        for i, ch in enumerate(chains):
+            r, _ = run_chain(ch, lat, xu, provider, c, PropagatorCache("device", c.block_length,
+                                                                      TorchBuffers(c)),
+                             chain=i, precision=hg.FP32)
+            alone.extend(r)
+        assert [(r.x, r.y, r.yv, r.chain) for r in res] == [(r.x, r.y, r.yv, r.chain) for r in alone]
+        assert [r.kernel_sum for r in res] == [r.kernel_sum for r in alone]
+        assert len(out22) == 1 and out22[0].chain == 0 and st.pieces_2p2 == 1

@@ -107,3 +107,19 @@ def test_empty_target_list():
     lat = [2, 2, 2, 2]
     p1, p234 = oracle_pieces_2p2(random_block(lat, 1), [0, 0, 0, 0], np.zeros((0, 4)), 1.0, lat)
     assert p234.shape == (0, 5, 64) and np.all(np.isfinite(p1))
+
+
+@pytest.mark.parametrize("case", golden_2p2()["plan_2p2"], ids=lambda c: c["name"])
+def test_plan_2p2_matches_reference(case):
+    """Which solves get the 2+2 over several chains (schedule.cpp:284-347):
+    the reference's plan and warning lines."""
+    from hlbl_gb300 import schedule
+
+    chains = [schedule.build_schedule(tuple(h), case["stride"], case["n_steps"], tuple(o))
+              for h, o in zip(case["h"], case["origins"])]
+    plan = schedule.plan_2p2(chains, [tuple(s) for s in case["sources"]], case["lattice"])
+    mine_at = sorted([c] + list(pos) + [idx] for c, d in enumerate(plan.at) for pos, idx in d.items())
+    assert mine_at == sorted(case["at"])
+    assert [list(p) + [c, w] for p, c, w in plan.not_sources] == case["not_sources"]
+    assert plan.unsolved == case["unsolved"]
+    assert schedule.report_2p2(plan, [tuple(s) for s in case["sources"]]) == case["report"]
