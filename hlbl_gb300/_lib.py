@@ -72,6 +72,7 @@ def _load() -> C.CDLL:
         "hlbl_autotune_f32": (C.c_int, [vp, vp, C.c_int, C.POINTER(vp), i4p, i4p, C.c_double, vp,
                                         C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]),
         "hlbl_ctx_set_qed_fp32": (C.c_int, [vp, C.c_int, C.c_double]),
+        "hlbl_ctx_set_p1f32_variant": (C.c_int, [vp, C.c_int, C.c_int]),
         "hlbl_ctx_reserve": (C.c_int, [vp, C.c_int]),
         "hlbl_stage_async": (C.c_int, [vp, vp, vp, C.c_size_t, C.c_int]),
         "hlbl_autotune": (C.c_int, [vp, vp, C.c_int, C.POINTER(vp), i4p, i4p, C.c_double, vp,

@@ -212,8 +212,13 @@ class Contractor:
         v, grp, ms = C.c_int(), C.c_int(), C.c_double()
         check(lib.hlbl_autotune_f32(self._h, ptr(d_y32), n, xs, g, y, C.c_double(xunit), ptr(d_out),
                                     C.byref(v), C.byref(grp), C.byref(ms)))
-        return {"p1": ("one stage, 2 CTAs/SM", "two stages, 1 CTA/SM")[v.value], "p2": "tensor-core",
+        return {"p1": ("one stage, 2 CTAs/SM", "two stages, 1 CTA/SM",
+                       "one flavour per CTA, two stages, 3 CTAs/SM")[v.value], "p2": "tensor-core",
                 "batch_group": grp.value, "ms": ms.value}
+
+    def set_p1f32_variant(self, variant: int, group: int = 0) -> None:
+        """The FP32-copy path's pass-1 variant (0, 1, 2) and pairs per launch."""
+        check(lib.hlbl_ctx_set_p1f32_variant(self._h, int(variant), int(group)))
 
     def f32_tile_copy(self, d_block, d_out) -> None:
         """The FP32 tile copy of a block (the tensor-core pass 2's input layout)."""

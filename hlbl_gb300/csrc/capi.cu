@@ -218,7 +218,7 @@ struct hlbl_ctx {
   // FP32 two-flavour pass 2 on the tensor cores (p2_tc.cu); off: CUDA cores
   int tc = 1;
   int grid_tc = 0;
-  int grid_p1f[2] = {0, 0};   // pass 1 on FP32 tile copies: 1 stage / 2 stages
+  int grid_p1f[kP1f32Variants] = {};  // pass 1 on FP32 tile copies, per variant (p2_tc.h)
   int p1f_var = 1;
   int group_f32 = 0;          // pairs per launch on the FP32-copy path (0: kMaxBatch)
   float* d_x32 = nullptr;     // FP32 tile copies: [1 + pair][f32 block] (y first)
@@ -342,7 +342,7 @@ int run_pass1(hlbl_ctx* c, const Geometry& geo, const double* y, const PairBatch
     else { grid = per_pair_grid(c->grid_p1f1, b.n, P1F1::tiles(geo.V)); P1F1::launch(grid, c->stream, y, b, geo, f0, c->d_part1, c->d_err); }
   }
   prof_end(c, 0);
-  p1_reduce_kernel<<<dim3((kDzLen + 255) / 256, nf, b.n), 256, 0, c->stream>>>(
+  p1_reduce_kernel<<<dim3((kDzLen + kRedOut - 1) / kRedOut, nf, b.n), kRedOut * kRedGrp, 0, c->stream>>>(
       c->d_part1, grid, nf, c->d_dz, add_dzu, add_dzsu);
   if (!build_bt) return HLBL_OK;
   g_build_kernel<<<dim3((kGLen / 2 + 255) / 256, nf, b.n), 256, 0, c->stream>>>(c->d_dz, nf, c->d_g);
@@ -420,7 +420,7 @@ int run_pass2(hlbl_ctx* c, const Geometry& geo, const double* y, const PairBatch
     else { grid = per_pair_grid(c->grid_p2f1, b.n, P2F1::tiles(geo.V)); P2F1::launch(grid, c->stream, y, b, geo, a, bt, c->d_part2, c->d_err); }
   }
   prof_end(c, 1);
-  p2_reduce_kernel<<<b.n, 32, 0, c->stream>>>(c->d_part2, grid, nf, b, add);
+  p2_reduce_kernel<<<b.n, 64, 0, c->stream>>>(c->d_part2, grid, nf, b, add);
   return HLBL_OK;
 }
 
@@ -439,7 +439,7 @@ int run_group_f32(hlbl_ctx* c, const PairBatch& b, const TcBatch& tb, double xun
   prof_begin(c, 0);
   p1f32_launch(v, g1, b.n, c->stream, tb, geo, c->d_part1, c->d_err);
   prof_end(c, 0);
-  p1_reduce_kernel<<<dim3((kDzLen + 255) / 256, 2, b.n), 256, 0, c->stream>>>(c->d_part1, g1, 2, c->d_dz,
+  p1_reduce_kernel<<<dim3((kDzLen + kRedOut - 1) / kRedOut, 2, b.n), kRedOut * kRedGrp, 0, c->stream>>>(c->d_part1, g1, 2, c->d_dz,
                                                                              nullptr, nullptr);
   g_build_kernel<<<dim3((kGLen / 2 + 255) / 256, 2, b.n), 256, 0, c->stream>>>(c->d_dz, 2, c->d_g);
   tc_launch_btu(c->d_g, b.n, c->d_btu, c->stream);
@@ -452,7 +452,7 @@ int run_group_f32(hlbl_ctx* c, const PairBatch& b, const TcBatch& tb, double xun
   prof_begin(c, 1);
   tc_launch_p2(g2, b.n, c->stream, tb, geo, a, c->d_btu, c->d_part2, c->d_err);
   prof_end(c, 1);
-  p2_reduce_kernel<<<b.n, 32, 0, c->stream>>>(c->d_part2, g2, 2, b, 0);
+  p2_reduce_kernel<<<b.n, 64, 0, c->stream>>>(c->d_part2, g2, 2, b, 0);
   return HLBL_OK;
 }
 
@@ -512,7 +512,7 @@ int hlbl_ctx_create(hlbl_ctx** out, const int global[4], const int local[4],
     return bail(rc);
   c->max_grid = std::max({c->grid_p1d2, c->grid_p1d1, c->grid_p1f2, c->grid_p1f1, c->grid_p2d2,
                           c->grid_p2d1, c->grid_p2f2, c->grid_p2f1, c->grid_p1f2s, c->grid_p2f2s,
-                          c->grid_tc, c->grid_p1f[0], c->grid_p1f[1]});
+                          c->grid_tc, c->grid_p1f[0], c->grid_p1f[1], c->grid_p1f[2]});
   e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->stage_ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->compute_ev, cudaEventDisableTiming);
@@ -659,7 +659,7 @@ int hlbl_autotune_f32(hlbl_ctx* c, const float* y32, int n, const float* const* 
   double best = 1e300;
   int bv = 1, bg = 1;
   int const groups[] = {1, 2, 4, 8, 16};
-  for (int v = 0; v < 2; ++v)
+  for (int v = 0; v < kP1f32Variants; ++v)
     for (int g : groups) {
       if (g > 1 && g / 2 >= n) continue;
       c->p1f_var = v;
@@ -736,6 +736,14 @@ int hlbl_ctx_set_qed_fp32(hlbl_ctx* c, int on, double r64) {
   if (!c || !(r64 >= 0)) return fail(HLBL_EINVAL, "hlbl_ctx_set_qed_fp32: bad argument");
   c->qed_fp32 = on ? 1 : 0;
   c->qed_r64 = r64;
+  return HLBL_OK;
+}
+
+int hlbl_ctx_set_p1f32_variant(hlbl_ctx* c, int variant, int group) {
+  if (!c || variant < 0 || variant >= kP1f32Variants || group < 0 || group > kMaxBatch)
+    return fail(HLBL_EINVAL, "hlbl_ctx_set_p1f32_variant: bad argument");
+  c->p1f_var = variant;
+  c->group_f32 = group;
   return HLBL_OK;
 }
 

@@ -351,21 +351,42 @@ p1_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, int f0,
 // Fixed-order, compensated (Neumaier) FP64 sum over the CTAs' partials.
 // dz[fl][i] = sum_cta partials[cta][fl][i]; if add_to != null also
 // add_to[fl][i] += dz (the reference's accumulate-into-caller semantics).
-static __global__ void p1_reduce_kernel(const double* __restrict__ partials, int ncta, int nf,
-                                 double* __restrict__ dz, double* add_dzu, double* add_dzsu) {
+// A CTA takes 32 outputs; its 8 warps each sum every 8th CTA's partials
+// (compensated), then one warp adds the 8 partial sums in order: 8x the
+// warps of one thread per output, each with an eighth of the chain.
+constexpr int kRedOut = 32, kRedGrp = 8;
+static __global__ void __launch_bounds__(kRedOut * kRedGrp)
+    p1_reduce_kernel(const double* __restrict__ partials, int ncta, int nf, double* __restrict__ dz,
+                     double* add_dzu, double* add_dzsu) {
   int const fl = blockIdx.y, pi = blockIdx.z;
-  int const i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= kDzLen || fl >= nf) return;
+  int const o = threadIdx.x % kRedOut, grp = threadIdx.x / kRedOut;
+  int const i = blockIdx.x * kRedOut + o;
+  __shared__ double rs[kRedGrp][kRedOut], rc[kRedGrp][kRedOut];
   partials += (size_t)pi * ncta * nf * kDzLen;
-  dz += (size_t)pi * nf * kDzLen;
   double s = 0.0, c = 0.0;
-  for (int b = 0; b < ncta; ++b) {
-    double const v = partials[((size_t)b * nf + fl) * kDzLen + i];
+  if (i < kDzLen && fl < nf) {
+    for (int b = grp; b < ncta; b += kRedGrp) {
+      double const v = partials[((size_t)b * nf + fl) * kDzLen + i];
+      double const tt = s + v;
+      c += fabs(s) >= fabs(v) ? (s - tt) + v : (v - tt) + s;
+      s = tt;
+    }
+  }
+  rs[grp][o] = s;
+  rc[grp][o] = c;
+  __syncthreads();
+  if (grp != 0 || i >= kDzLen || fl >= nf) return;
+  s = 0.0;
+  c = 0.0;
+  for (int g = 0; g < kRedGrp; ++g) {
+    c += rc[g][o];
+    double const v = rs[g][o];
     double const tt = s + v;
     c += fabs(s) >= fabs(v) ? (s - tt) + v : (v - tt) + s;
     s = tt;
   }
   s += c;
+  dz += (size_t)pi * nf * kDzLen;
   dz[fl * kDzLen + i] = s;
   if (add_dzu != nullptr) {
     if (i < kDzuLen) add_dzu[fl * kDzuLen + i] += s;
@@ -885,20 +906,36 @@ p2_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, P2Args ar
 
 // out[fl] = sum_cta partials[cta][fl] (fixed order, compensated); if add
 // is set, out[fl] is added to rather than written.
-static __global__ void p2_reduce_kernel(const double* __restrict__ partials, int ncta, int nf,
-                                        PairBatch batch, int add) {
-  int const fl = threadIdx.x, pi = blockIdx.x;
+// One warp per flavour: lane l sums every 32nd CTA's partial (compensated),
+// lane 0 adds the 32 lane sums in order (fixed order, deterministic).
+static __global__ void __launch_bounds__(64) p2_reduce_kernel(const double* __restrict__ partials, int ncta,
+                                                              int nf, PairBatch batch, int add) {
+  int const fl = threadIdx.x >> 5, lane = threadIdx.x & 31, pi = blockIdx.x;
+  __shared__ double rs[2][32], rc[2][32];
   if (fl >= nf) return;
-  double* __restrict__ out = batch.p[pi].out;
   partials += (size_t)pi * ncta * nf;
   double s = 0.0, c = 0.0;
-  for (int b = 0; b < ncta; ++b) {
+  for (int b = lane; b < ncta; b += 32) {
     double const v = partials[(size_t)b * nf + fl];
     double const tt = s + v;
     c += fabs(s) >= fabs(v) ? (s - tt) + v : (v - tt) + s;
     s = tt;
   }
+  rs[fl][lane] = s;
+  rc[fl][lane] = c;
+  __syncwarp();
+  if (lane != 0) return;
+  s = 0.0;
+  c = 0.0;
+  for (int l = 0; l < 32; ++l) {
+    c += rc[fl][l];
+    double const v = rs[fl][l];
+    double const tt = s + v;
+    c += fabs(s) >= fabs(v) ? (s - tt) + v : (v - tt) + s;
+    s = tt;
+  }
   s += c;
+  double* __restrict__ out = batch.p[pi].out;
   if (add) out[fl] += s;
   else out[fl] = s;
 }

@@ -10,9 +10,11 @@
 // coordinates, dzu[k]; per-tile FP32 sums go into Kahan FP32 accumulators,
 // converted to FP64 at the end; partials per CTA in p1_kernel's layout.
 // A tile is half of a 32-site tile of the copy (16 sites): one 1.5 KB TMA
-// copy per row (48 rows). ST = 1: one stage per CTA, two CTAs per SM (the
-// other CTA computes while one waits); ST = 2: two stages, the next tile
-// prefetched while this one is computed, one CTA per SM.
+// copy per row. NFL = 2: a CTA of 288 threads takes both flavours (48 rows);
+// ST = 1: one stage, two CTAs per SM (the other CTA computes while one
+// waits); ST = 2: two stages (the next tile prefetched while this one is
+// computed), one CTA per SM. NFL = 1: a CTA of 144 threads takes one flavour
+// (blockIdx.y = 2 pair + flavour, 24 rows), two stages, three CTAs per SM.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -26,40 +28,46 @@ namespace hg {
 namespace p1f {
 
 constexpr int kTS = 16;                   // sites per tile (half of a copy tile)
-constexpr int kRows = 48;                 // (x, y) x 2 flavours x 12
 constexpr int kRowFloats = kTS * 24;      // 384: [c4][16][4]
 constexpr uint32_t kRowBytes = kRowFloats * 4;
 // staged rows 16 bytes apart more than their length, so that the rows the
 // threads of one warp read (12 y rows, 3 x rows) start in different banks
 constexpr int kRowStride = kRowFloats + 4;
-constexpr int kThreads = 2 * 144;
+template <int NFL> __host__ __device__ constexpr int rows() { return 24 * NFL; }   // (x, y) x flavours x 12
+template <int NFL> __host__ __device__ constexpr int threads() { return 144 * NFL; }
+template <int ST, int NFL> __host__ __device__ constexpr int min_ctas() { return NFL == 1 ? 3 : (ST == 1 ? 2 : 1); }
 
-template <int ST>
+template <int ST, int NFL>
 struct Smem {
-  float stage[ST][kRows][kRowStride];
+  float stage[ST][rows<NFL>()][kRowStride];
   float zh[kTS][4];
 };
 
-template <int ST>
-__global__ void __launch_bounds__(kThreads, ST == 1 ? 2 : 1)
+template <int ST, int NFL>
+__global__ void __launch_bounds__(threads<NFL>(), min_ctas<ST, NFL>())
 p1f32_kernel(TcBatch tb, Geometry geo, double* __restrict__ partials, int* __restrict__ err) {
+  constexpr int kRows = rows<NFL>();
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  Smem<ST>& sm = *reinterpret_cast<Smem<ST>*>(smem_raw);
+  Smem<ST, NFL>& sm = *reinterpret_cast<Smem<ST, NFL>*>(smem_raw);
   __shared__ __align__(8) uint64_t s_bar[ST];
   __shared__ int s_fail;
-  int const t = threadIdx.x, pi = blockIdx.y;
-  int const fl = t / 144, ia = (t % 144) / 12, ib = t % 12;
+  int const t = threadIdx.x;
+  // NFL = 1: blockIdx.y = 2 pair + flavour; the CTA's rows are that flavour's
+  int const pi = NFL == 1 ? blockIdx.y >> 1 : blockIdx.y;
+  int const fl = NFL == 1 ? (int)(blockIdx.y & 1) : t / 144;
+  int const ia = (t % 144) / 12, ib = t % 12;
   const float* __restrict__ x32 = tb.x32[pi];
   const float* __restrict__ y32 = tb.y32;
   int const gsx[4] = {tb.gsx[pi][0], tb.gsx[pi][1], tb.gsx[pi][2], tb.gsx[pi][3]};
   long long const nt32 = (geo.V + 31) / 32;
   long long const ntiles = (geo.V + kTS - 1) / kTS;
   // rows: which = 0 x at flavour fl, which = 1 y at flavour 1 - fl
+  // (NFL = 2: [which][f][12]; NFL = 1: [which][12] of the CTA's flavour)
   auto issue = [&](long long tile, int st) {
     mbar_arrive_expect_tx(&s_bar[st], kRows * kRowBytes);
     long long const t32 = tile >> 1, half = tile & 1;
     for (int row = 0; row < kRows; ++row) {
-      int const which = row / 24, f = (row / 12) % 2, i = row % 12;
+      int const which = row / (12 * NFL), f = NFL == 1 ? fl : (row / 12) % 2, i = row % 12;
       int const ff = which == 0 ? f : 1 - f;
       const float* src = (which == 0 ? x32 : y32) + ((size_t)(ff * 12 + i) * nt32 + t32) * kRowF32 + half * kRowFloats;
       bulk_g2s(sm.stage[st][row], src, kRowBytes, &s_bar[st]);
@@ -85,8 +93,8 @@ p1f32_kernel(TcBatch tb, Geometry geo, double* __restrict__ partials, int* __res
       fence_proxy_async_smem();
       issue(tile + gridDim.x, st ^ 1);
     }
-    const float* Arow = sm.stage[st][0 * 24 + fl * 12 + ia];
-    const float* Brow = sm.stage[st][1 * 24 + fl * 12 + ib];
+    const float* Arow = sm.stage[st][NFL == 1 ? ia : fl * 12 + ia];
+    const float* Brow = sm.stage[st][NFL == 1 ? 12 + ib : 24 + fl * 12 + ib];
     long long const s0 = tile * kTS;
     int const nvalid = (int)min((long long)kTS, geo.V - s0);
     for (int it = t; it < kTS * 4; it += blockDim.x) {
@@ -187,25 +195,28 @@ p1f32_kernel(TcBatch tb, Geometry geo, double* __restrict__ partials, int* __res
 
 }  // namespace p1f
 
-template <int ST>
+template <int ST, int NFL>
 int p1f32_init_t(int nsm, int& grid) {
-  size_t const smem = sizeof(p1f::Smem<ST>);
-  cudaError_t e = cudaFuncSetAttribute(p1f::p1f32_kernel<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  size_t const smem = sizeof(p1f::Smem<ST, NFL>);
+  cudaError_t e = cudaFuncSetAttribute(p1f::p1f32_kernel<ST, NFL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(p1f::p1f32_kernel<ST>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    e = cudaFuncSetAttribute(p1f::p1f32_kernel<ST, NFL>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return cuda_fail(e, "p1f32 smem attribute");
   int nb = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, p1f::p1f32_kernel<ST>, p1f::kThreads, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, p1f::p1f32_kernel<ST, NFL>, p1f::threads<NFL>(), smem);
   if (e != cudaSuccess) return cuda_fail(e, "p1f32 occupancy");
   if (nb < 1) return fail(HLBL_ECUDA, "p1f32 kernel cannot be resident");
-  grid = nb * nsm;
+  // NFL = 1 launches two CTAs (one per flavour) per tile range: the same
+  // number of CTAs per pair as NFL = 2 at its occupancy
+  grid = NFL == 1 ? (nb * nsm) / 2 : nb * nsm;
   return HLBL_OK;
 }
 
-int p1f32_init(int nsm, int grid[2]) {
-  if (int rc = p1f32_init_t<1>(nsm, grid[0])) return rc;
-  return p1f32_init_t<2>(nsm, grid[1]);
+int p1f32_init(int nsm, int grid[kP1f32Variants]) {
+  if (int rc = p1f32_init_t<1, 2>(nsm, grid[0])) return rc;
+  if (int rc = p1f32_init_t<2, 2>(nsm, grid[1])) return rc;
+  return p1f32_init_t<2, 1>(nsm, grid[2]);
 }
 
 long long p1f32_tiles(long long V) { return (V + p1f::kTS - 1) / p1f::kTS; }
@@ -213,9 +224,11 @@ long long p1f32_tiles(long long V) { return (V + p1f::kTS - 1) / p1f::kTS; }
 void p1f32_launch(int variant, int grid, int npairs, cudaStream_t st, const TcBatch& tb, const Geometry& geo,
                   double* partials, int* err) {
   if (variant == 0)
-    p1f::p1f32_kernel<1><<<dim3(grid, npairs), p1f::kThreads, sizeof(p1f::Smem<1>), st>>>(tb, geo, partials, err);
+    p1f::p1f32_kernel<1, 2><<<dim3(grid, npairs), p1f::threads<2>(), sizeof(p1f::Smem<1, 2>), st>>>(tb, geo, partials, err);
+  else if (variant == 1)
+    p1f::p1f32_kernel<2, 2><<<dim3(grid, npairs), p1f::threads<2>(), sizeof(p1f::Smem<2, 2>), st>>>(tb, geo, partials, err);
   else
-    p1f::p1f32_kernel<2><<<dim3(grid, npairs), p1f::kThreads, sizeof(p1f::Smem<2>), st>>>(tb, geo, partials, err);
+    p1f::p1f32_kernel<2, 1><<<dim3(grid, 2 * npairs), p1f::threads<1>(), sizeof(p1f::Smem<2, 1>), st>>>(tb, geo, partials, err);
 }
 
 }  // namespace hg

@@ -38,8 +38,11 @@ void tc_launch_p2(int grid, int npairs, cudaStream_t st, const TcBatch& tb, cons
 long long tc_tiles(long long V);
 
 // Pass 1 on FP32 tile copies (p1_f32.cu); partials in p1_kernel's layout.
-// variant 0: one stage, two CTAs per SM; 1: two stages, one CTA per SM
-int p1f32_init(int nsm, int grid[2]);
+// variant 0: both flavours per CTA, one stage, two CTAs per SM; 1: both
+// flavours, two stages, one CTA per SM; 2: one flavour per CTA, two stages,
+// three CTAs per SM
+constexpr int kP1f32Variants = 3;
+int p1f32_init(int nsm, int grid[kP1f32Variants]);
 long long p1f32_tiles(long long V);
 void p1f32_launch(int variant, int grid, int npairs, cudaStream_t st, const TcBatch& tb, const Geometry& geo,
                   double* partials, int* err);

@@ -146,12 +146,24 @@ def test_f32_copy_path_matches_oracle_and_fp64_input_path(lat):
         c.kernel_sums_batched_f32(y32, x32, gsxs, yvs, xu, out)
         ref = torch.zeros_like(out)
         c.kernel_sums_batched(d_y, d_srcs, gsxs, yvs, xu, ref, hg.FP32)
+        # every pass-1 variant and pair grouping gives the same sums (the
+        # per-thread order of the FP32 sums is the same; CTA counts differ)
+        per_var = []
+        for v in range(3):
+            for g in (1, 3):
+                c.set_p1f32_variant(v, g)
+                o = torch.zeros_like(out)
+                c.kernel_sums_batched_f32(y32, x32, gsxs, yvs, xu, o)
+                per_var.append(o.cpu().numpy())
         tuned = torch.zeros_like(out)
         best = c.autotune_f32(y32, x32, gsxs, yvs, xu, tuned)
         c.kernel_sums_batched_f32(y32, x32, gsxs, yvs, xu, tuned)
         c.check()
         got, r64, tun = out.cpu().numpy(), ref.cpu().numpy(), tuned.cpu().numpy()
     assert best["batch_group"] in (1, 2, 4, 8, 16)
+    for o in per_var:
+        for i in range(3):
+            assert S.pair_rel_err(o[i], got[i]) <= 1e-6
     for i in range(3):
         orc = S.oracle_kernel_sum(srcs[i], y, gsxs[i], yvs[i], xu, lat)
         assert S.pair_rel_err(got[i], orc) <= TOL32
