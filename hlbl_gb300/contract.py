@@ -213,7 +213,9 @@ class Contractor:
         check(lib.hlbl_autotune_f32(self._h, ptr(d_y32), n, xs, g, y, C.c_double(xunit), ptr(d_out),
                                     C.byref(v), C.byref(grp), C.byref(ms)))
         return {"p1": ("one stage, 2 CTAs/SM", "two stages, 1 CTA/SM",
-                       "one flavour per CTA, two stages, 3 CTAs/SM")[v.value], "p2": "tensor-core",
+                       "one flavour per CTA, two stages, 3 CTAs/SM",
+                       "one flavour per CTA, producer warp, empty/full barriers")[v.value],
+                "p2": "tensor-core",
                 "batch_group": grp.value, "ms": ms.value}
 
     def set_p1f32_variant(self, variant: int, group: int = 0) -> None:

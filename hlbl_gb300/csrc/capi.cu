@@ -512,7 +512,7 @@ int hlbl_ctx_create(hlbl_ctx** out, const int global[4], const int local[4],
     return bail(rc);
   c->max_grid = std::max({c->grid_p1d2, c->grid_p1d1, c->grid_p1f2, c->grid_p1f1, c->grid_p2d2,
                           c->grid_p2d1, c->grid_p2f2, c->grid_p2f1, c->grid_p1f2s, c->grid_p2f2s,
-                          c->grid_tc, c->grid_p1f[0], c->grid_p1f[1], c->grid_p1f[2]});
+                          c->grid_tc, c->grid_p1f[0], c->grid_p1f[1], c->grid_p1f[2], c->grid_p1f[3]});
   e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->stage_ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->compute_ev, cudaEventDisableTiming);

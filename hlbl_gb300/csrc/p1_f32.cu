@@ -37,6 +37,70 @@ template <int NFL> __host__ __device__ constexpr int rows() { return 24 * NFL; }
 template <int NFL> __host__ __device__ constexpr int threads() { return 144 * NFL; }
 template <int ST, int NFL> __host__ __device__ constexpr int min_ctas() { return NFL == 1 ? 3 : (ST == 1 ? 2 : 1); }
 
+// One tile's contribution of thread (fl, ia, ib): per site the eight
+// spin-block products, X_sigma, and the zerohalf-weighted sums, summed over
+// the tile in FP32 and added into the Kahan accumulators.
+__device__ __forceinline__ void tile_sums(const float* __restrict__ Arow, const float* __restrict__ Brow,
+                                          const float (*zhs)[4], int nvalid, KahanF (&acc_u)[6][2],
+                                          KahanF (&acc_s)[4][2]) {
+    float tu[6][2], ts[4][2];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) tu[k][0] = tu[k][1] = 0.f;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) ts[s][0] = ts[s][1] = 0.f;
+#pragma unroll 1
+    for (int s = 0; s < nvalid; ++s) {
+      float A[24], B[24];
+#pragma unroll
+      for (int c4 = 0; c4 < 6; ++c4) {
+        float4 const a = *reinterpret_cast<const float4*>(Arow + c4 * 64 + s * 4);
+        float4 const b = *reinterpret_cast<const float4*>(Brow + c4 * 64 + s * 4);
+        A[4 * c4] = a.x; A[4 * c4 + 1] = a.y; A[4 * c4 + 2] = a.z; A[4 * c4 + 3] = a.w;
+        B[4 * c4] = b.x; B[4 * c4 + 1] = b.y; B[4 * c4 + 2] = b.z; B[4 * c4 + 3] = b.w;
+      }
+      // P[s1][s2] = sum_c conj(B[s1][c]) A[s2][c] for s2 = s1^2 and 3-s1
+      float pa[4][2], pb[4][2];
+#pragma unroll
+      for (int s1 = 0; s1 < 4; ++s1) {
+        float ar = 0, ai = 0, br = 0, bi = 0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          float const yr = B[2 * (3 * s1 + c)], yi = B[2 * (3 * s1 + c) + 1];
+          int const sa = 2 * (3 * (s1 ^ 2) + c), sb = 2 * (3 * (3 - s1) + c);
+          ar += yr * A[sa] + yi * A[sa + 1];  ai += yr * A[sa + 1] - yi * A[sa];
+          br += yr * A[sb] + yi * A[sb + 1];  bi += yr * A[sb + 1] - yi * A[sb];
+        }
+        pa[s1][0] = ar; pa[s1][1] = ai; pb[s1][0] = br; pb[s1][1] = bi;
+      }
+      float X[4][2];
+#pragma unroll
+      for (int sg = 0; sg < 4; ++sg) {
+        float xr = 0, xi = 0;
+#pragma unroll
+        for (int s1 = 0; s1 < 4; ++s1) {
+          float const* pp = (sg == 0 || sg == 3) ? pa[s1] : pb[s1];
+          float vr, vi;
+          mul_iph(g5g_ph(sg, s1), pp[0], pp[1], vr, vi);
+          xr += vr; xi += vi;
+        }
+        X[sg][0] = xr; X[sg][1] = xi;
+      }
+#pragma unroll
+      for (int sg = 0; sg < 4; ++sg) { ts[sg][0] += X[sg][0]; ts[sg][1] += X[sg][1]; }
+      const float* zh = zhs[s];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        int const r = comb_rho(k), g = comb_sigma(k);
+        tu[k][0] += zh[r] * X[g][0] - zh[g] * X[r][0];
+        tu[k][1] += zh[r] * X[g][1] - zh[g] * X[r][1];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) { acc_u[k][0].add(tu[k][0]); acc_u[k][1].add(tu[k][1]); }
+#pragma unroll
+    for (int s = 0; s < 4; ++s) { acc_s[s][0].add(ts[s][0]); acc_s[s][1].add(ts[s][1]); }
+}
+
 template <int ST, int NFL>
 struct Smem {
   float stage[ST][rows<NFL>()][kRowStride];
@@ -106,62 +170,7 @@ p1f32_kernel(TcBatch tb, Geometry geo, double* __restrict__ partials, int* __res
     if (!mbar_wait(&s_bar[st], parity)) s_fail = 1;
     __syncthreads();
     if (s_fail) break;
-    float tu[6][2], ts[4][2];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) tu[k][0] = tu[k][1] = 0.f;
-#pragma unroll
-    for (int s = 0; s < 4; ++s) ts[s][0] = ts[s][1] = 0.f;
-#pragma unroll 1
-    for (int s = 0; s < nvalid; ++s) {
-      float A[24], B[24];
-#pragma unroll
-      for (int c4 = 0; c4 < 6; ++c4) {
-        float4 const a = *reinterpret_cast<const float4*>(Arow + c4 * 64 + s * 4);
-        float4 const b = *reinterpret_cast<const float4*>(Brow + c4 * 64 + s * 4);
-        A[4 * c4] = a.x; A[4 * c4 + 1] = a.y; A[4 * c4 + 2] = a.z; A[4 * c4 + 3] = a.w;
-        B[4 * c4] = b.x; B[4 * c4 + 1] = b.y; B[4 * c4 + 2] = b.z; B[4 * c4 + 3] = b.w;
-      }
-      // P[s1][s2] = sum_c conj(B[s1][c]) A[s2][c] for s2 = s1^2 and 3-s1
-      float pa[4][2], pb[4][2];
-#pragma unroll
-      for (int s1 = 0; s1 < 4; ++s1) {
-        float ar = 0, ai = 0, br = 0, bi = 0;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          float const yr = B[2 * (3 * s1 + c)], yi = B[2 * (3 * s1 + c) + 1];
-          int const sa = 2 * (3 * (s1 ^ 2) + c), sb = 2 * (3 * (3 - s1) + c);
-          ar += yr * A[sa] + yi * A[sa + 1];  ai += yr * A[sa + 1] - yi * A[sa];
-          br += yr * A[sb] + yi * A[sb + 1];  bi += yr * A[sb + 1] - yi * A[sb];
-        }
-        pa[s1][0] = ar; pa[s1][1] = ai; pb[s1][0] = br; pb[s1][1] = bi;
-      }
-      float X[4][2];
-#pragma unroll
-      for (int sg = 0; sg < 4; ++sg) {
-        float xr = 0, xi = 0;
-#pragma unroll
-        for (int s1 = 0; s1 < 4; ++s1) {
-          float const* pp = (sg == 0 || sg == 3) ? pa[s1] : pb[s1];
-          float vr, vi;
-          mul_iph(g5g_ph(sg, s1), pp[0], pp[1], vr, vi);
-          xr += vr; xi += vi;
-        }
-        X[sg][0] = xr; X[sg][1] = xi;
-      }
-#pragma unroll
-      for (int sg = 0; sg < 4; ++sg) { ts[sg][0] += X[sg][0]; ts[sg][1] += X[sg][1]; }
-      const float* zh = sm.zh[s];
-#pragma unroll
-      for (int k = 0; k < 6; ++k) {
-        int const r = comb_rho(k), g = comb_sigma(k);
-        tu[k][0] += zh[r] * X[g][0] - zh[g] * X[r][0];
-        tu[k][1] += zh[r] * X[g][1] - zh[g] * X[r][1];
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < 6; ++k) { acc_u[k][0].add(tu[k][0]); acc_u[k][1].add(tu[k][1]); }
-#pragma unroll
-    for (int s = 0; s < 4; ++s) { acc_s[s][0].add(ts[s][0]); acc_s[s][1].add(ts[s][1]); }
+    tile_sums(Arow, Brow, sm.zh, nvalid, acc_u, acc_s);
     __syncthreads();  // the stage and zh are rewritten for the next tile
     if (ST == 1 && t == 0 && tile + gridDim.x < ntiles) {
       fence_proxy_async_smem();
@@ -180,6 +189,127 @@ p1f32_kernel(TcBatch tb, Geometry geo, double* __restrict__ partials, int* __res
     }
     return;
   }
+  double* out = partials + (((size_t)pi * gridDim.x + blockIdx.x) * 2 + fl) * kDzLen;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    out[((k * 12 + ia) * 12 + ib) * 2] = acc_u[k][0].get();
+    out[((k * 12 + ia) * 12 + ib) * 2 + 1] = acc_u[k][1].get();
+  }
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    out[kDzuLen + ((s * 12 + ia) * 12 + ib) * 2] = acc_s[s][0].get();
+    out[kDzuLen + ((s * 12 + ia) * 12 + ib) * 2 + 1] = acc_s[s][1].get();
+  }
+}
+
+
+// ---- warp-specialized form (variant 3): one flavour per CTA, a producer
+// warp and empty/full mbarriers per stage instead of a block barrier per tile.
+// Warps 0-4 compute (threads 0..143, (ia, ib)); warp 5 computes each tile's
+// zerohalf weights and issues its TMA copies. A stage is refilled once all
+// five compute warps have released it, so a warp may run a tile ahead.
+constexpr int kWsStages = 2;
+constexpr int kWsThreads = 192;
+constexpr int kWsComputeWarps = 5;
+
+struct SmemWs {
+  float stage[kWsStages][24][kRowStride];
+  float zh[kWsStages][kTS][4];
+};
+
+__device__ __forceinline__ void mbar_arrive_local(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// three CTAs of 192 threads per SM: at most 104 registers a thread
+__global__ void __maxnreg__(104)
+p1f32_ws_kernel(TcBatch tb, Geometry geo, double* __restrict__ partials, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  SmemWs& sm = *reinterpret_cast<SmemWs*>(smem_raw);
+  __shared__ __align__(8) uint64_t s_full[kWsStages], s_empty[kWsStages];
+  __shared__ int s_fail;
+  int const t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  int const pi = blockIdx.y >> 1, fl = (int)(blockIdx.y & 1);
+  int const ia = (t % 144) / 12, ib = t % 12;
+  long long const ntiles = (geo.V + kTS - 1) / kTS;
+  if (t == 0) {
+    for (int i = 0; i < kWsStages; ++i) {
+      mbar_init(&s_full[i], 32);  // the producer warp's lanes (lane 0 with the bytes)
+      mbar_init(&s_empty[i], kWsComputeWarps);
+    }
+    fence_mbar_init();
+    s_fail = 0;
+  }
+  __syncthreads();
+  volatile int* fail = &s_fail;
+  KahanF acc_u[6][2], acc_s[4][2];
+  long long last[kWsStages] = {-1, -1};  // producer: the last tile issued into each stage
+  if (warp == kWsComputeWarps) {
+    // ---- producer ----
+    const float* __restrict__ x32 = tb.x32[pi];
+    const float* __restrict__ y32 = tb.y32;
+    int const gsx[4] = {tb.gsx[pi][0], tb.gsx[pi][1], tb.gsx[pi][2], tb.gsx[pi][3]};
+    long long const nt32 = (geo.V + 31) / 32;
+    int it = 0;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+      int const st = it % kWsStages;
+      // stage st is free once the five compute warps released its previous tile
+      if (it >= kWsStages && !mbar_wait(&s_empty[st], (uint32_t)((it / kWsStages - 1) & 1))) {
+        *fail = 1;
+        break;
+      }
+      if (*fail) break;
+      long long const s0 = tile * kTS;
+      for (int i = lane; i < kTS * 4; i += 32) {
+        int const s = i >> 2, r = i & 3;
+        int rel[4];
+        rel_coords(geo, gsx, min(s0 + s, geo.V - 1), rel);
+        sm.zh[st][s][r] = (float)coord_map_zerohalf(rel[r], geo.global[r]);
+      }
+      if (lane == 0) {
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&s_full[st], 24 * kRowBytes);
+        long long const t32 = tile >> 1, half = tile & 1;
+        for (int row = 0; row < 24; ++row) {
+          int const which = row / 12, i = row % 12, ff = which == 0 ? fl : 1 - fl;
+          const float* src = (which == 0 ? x32 : y32) + ((size_t)(ff * 12 + i) * nt32 + t32) * kRowF32 +
+                             half * kRowFloats;
+          bulk_g2s(sm.stage[st][row], src, kRowBytes, &s_full[st]);
+        }
+        last[st] = it;
+      } else {
+        mbar_arrive_local(&s_full[st]);  // releases this lane's zero-half weights
+      }
+    }
+  } else {
+    // ---- compute warps ----
+    int it = 0;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+      int const st = it % kWsStages;
+      if (!mbar_wait(&s_full[st], (uint32_t)((it / kWsStages) & 1))) {
+        *fail = 1;
+        break;
+      }
+      if (*fail) break;
+      if (t < 144) {
+        int const nvalid = (int)min((long long)kTS, geo.V - tile * kTS);
+        tile_sums(sm.stage[st][ia], sm.stage[st][12 + ib], sm.zh[st], nvalid, acc_u, acc_s);
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive_local(&s_empty[st]);
+    }
+  }
+  __syncthreads();
+  if (*fail) {
+    // a wait gave up: report it; the producer lets every copy in flight land
+    // before the CTA exits (bounded)
+    if (t == 0 && err) atomicExch(err, kErrWaitTimeout);
+    if (warp == kWsComputeWarps && lane == 0)
+      for (int st = 0; st < kWsStages; ++st)
+        if (last[st] >= 0) mbar_wait(&s_full[st], (uint32_t)((last[st] / kWsStages) & 1));
+    return;
+  }
+  if (t >= 144) return;
   double* out = partials + (((size_t)pi * gridDim.x + blockIdx.x) * 2 + fl) * kDzLen;
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
@@ -213,10 +343,26 @@ int p1f32_init_t(int nsm, int& grid) {
   return HLBL_OK;
 }
 
+int p1f32_init_ws(int nsm, int& grid) {
+  size_t const smem = sizeof(p1f::SmemWs);
+  cudaError_t e = cudaFuncSetAttribute(p1f::p1f32_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(p1f::p1f32_ws_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return cuda_fail(e, "p1f32 smem attribute");
+  int nb = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, p1f::p1f32_ws_kernel, p1f::kWsThreads, smem);
+  if (e != cudaSuccess) return cuda_fail(e, "p1f32 occupancy");
+  if (nb < 1) return fail(HLBL_ECUDA, "p1f32 kernel cannot be resident");
+  grid = (nb * nsm) / 2;  // two CTAs (one per flavour) per tile range
+  return HLBL_OK;
+}
+
 int p1f32_init(int nsm, int grid[kP1f32Variants]) {
   if (int rc = p1f32_init_t<1, 2>(nsm, grid[0])) return rc;
   if (int rc = p1f32_init_t<2, 2>(nsm, grid[1])) return rc;
-  return p1f32_init_t<2, 1>(nsm, grid[2]);
+  if (int rc = p1f32_init_t<2, 1>(nsm, grid[2])) return rc;
+  return p1f32_init_ws(nsm, grid[3]);
 }
 
 long long p1f32_tiles(long long V) { return (V + p1f::kTS - 1) / p1f::kTS; }
@@ -227,8 +373,10 @@ void p1f32_launch(int variant, int grid, int npairs, cudaStream_t st, const TcBa
     p1f::p1f32_kernel<1, 2><<<dim3(grid, npairs), p1f::threads<2>(), sizeof(p1f::Smem<1, 2>), st>>>(tb, geo, partials, err);
   else if (variant == 1)
     p1f::p1f32_kernel<2, 2><<<dim3(grid, npairs), p1f::threads<2>(), sizeof(p1f::Smem<2, 2>), st>>>(tb, geo, partials, err);
-  else
+  else if (variant == 2)
     p1f::p1f32_kernel<2, 1><<<dim3(grid, 2 * npairs), p1f::threads<1>(), sizeof(p1f::Smem<2, 1>), st>>>(tb, geo, partials, err);
+  else
+    p1f::p1f32_ws_kernel<<<dim3(grid, 2 * npairs), p1f::kWsThreads, sizeof(p1f::SmemWs), st>>>(tb, geo, partials, err);
 }
 
 }  // namespace hg

@@ -40,8 +40,9 @@ long long tc_tiles(long long V);
 // Pass 1 on FP32 tile copies (p1_f32.cu); partials in p1_kernel's layout.
 // variant 0: both flavours per CTA, one stage, two CTAs per SM; 1: both
 // flavours, two stages, one CTA per SM; 2: one flavour per CTA, two stages,
-// three CTAs per SM
-constexpr int kP1f32Variants = 3;
+// three CTAs per SM; 3: as 2 with a producer warp and per-stage empty/full
+// mbarriers instead of a block barrier per tile
+constexpr int kP1f32Variants = 4;
 int p1f32_init(int nsm, int grid[kP1f32Variants]);
 long long p1f32_tiles(long long V);
 void p1f32_launch(int variant, int grid, int npairs, cudaStream_t st, const TcBatch& tb, const Geometry& geo,

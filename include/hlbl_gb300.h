@@ -143,14 +143,15 @@ int hlbl_kernel_sums_batched_f32(hlbl_ctx* ctx, const float* d_y32, int n, const
 
 /* Autotuner of the FP32-copy path: pass-1 variant (0: both flavours per CTA,
  * one stage, two CTAs per SM; 1: both flavours, two stages, one CTA per SM;
- * 2: one flavour per CTA, two stages, three CTAs per SM) and pairs per
- * launch (1, 2, 4, 8, 16),
+ * 2: one flavour per CTA, two stages, three CTAs per SM; 3: as 2 with a
+ * producer warp and per-stage empty/full barriers) and pairs per launch
+ * (1, 2, 4, 8, 16),
  * timed on one batch; keeps the fastest. Blocking. No counterpart in the
  * reference. */
 int hlbl_autotune_f32(hlbl_ctx* ctx, const float* d_y32, int n, const float* const* d_x32s,
                       const int* gsx, const int* yv, double xunit, double* d_out, int* best_variant,
                       int* best_group, double* best_ms);
-/* Set what hlbl_autotune_f32 chooses: the pass-1 variant (0, 1, 2 as above)
+/* Set what hlbl_autotune_f32 chooses: the pass-1 variant (0-3 as above)
  * and the pairs per launch (0: 16). */
 int hlbl_ctx_set_p1f32_variant(hlbl_ctx* ctx, int variant, int group);
 

@@ -149,7 +149,7 @@ def test_f32_copy_path_matches_oracle_and_fp64_input_path(lat):
         # every pass-1 variant and pair grouping gives the same sums (the
         # per-thread order of the FP32 sums is the same; CTA counts differ)
         per_var = []
-        for v in range(3):
+        for v in range(4):
             for g in (1, 3):
                 c.set_p1f32_variant(v, g)
                 o = torch.zeros_like(out)
