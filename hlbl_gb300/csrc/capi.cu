@@ -106,17 +106,24 @@ __global__ void wait_timeout_selftest_kernel(int* err) {
 
 // The FP32 tile copy of one block ([f][ia][tile][2][6][16][4] floats), with the
 // conversion pass 1 uses; sites past V in the last tile are left untouched.
+// FP64 block -> FP32 tile copy. A warp takes one (row, 32-site tile, 16-byte
+// group c4): lane = site of the tile, so each lane reads one 32-byte sector
+// of the block and the warp writes two contiguous 256-byte runs of the copy;
+// 32-bit index arithmetic (V * 6 < 2^31), blockIdx.y = row (f, ia).
 __global__ void f32_tile_copy_kernel(const double* __restrict__ blk, Geometry geo, float* __restrict__ out) {
-  long long const n = geo.V * 24 * 6;  // (f, ia, site, c4)
-  long long const nt32 = (geo.V + 31) / 32;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    int const c4 = (int)(i % 6);
-    long long const site = (i / 6) % geo.V;
-    int const row = (int)(i / (6 * geo.V));  // f*12 + ia
-    const double* src = blk + ((size_t)row * geo.V + site) * 24 + 4 * c4;
-    float4 const v = make_float4(f64_to_f32(src[0]), f64_to_f32(src[1]), f64_to_f32(src[2]), f64_to_f32(src[3]));
-    *reinterpret_cast<float4*>(out + ((size_t)row * nt32 + (site >> 5)) * (32 * 24) + f32_tile_off((int)(site & 31), c4)) = v;
+  unsigned const nt32 = (unsigned)((geo.V + 31) / 32), V = (unsigned)geo.V;
+  unsigned const n = nt32 * 6 * 32;  // (tile, c4, lane)
+  int const row = blockIdx.y;
+  const double* __restrict__ src_row = blk + (size_t)row * geo.V * 24;
+  float* __restrict__ dst_row = out + (size_t)row * nt32 * (32 * 24);
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    unsigned const lane = i & 31, k = i >> 5, c4 = k % 6, t32 = k / 6;
+    unsigned const site = t32 * 32 + lane;
+    if (site >= V) continue;  // the copy's padding past the last site is never read
+    const double2* src = reinterpret_cast<const double2*>(src_row + (size_t)site * 24 + 4 * c4);
+    double2 const v0 = src[0], v1 = src[1];
+    *reinterpret_cast<float4*>(dst_row + (size_t)t32 * (32 * 24) + f32_tile_off((int)lane, (int)c4)) =
+        make_float4(f64_to_f32(v0.x), f64_to_f32(v0.y), f64_to_f32(v1.x), f64_to_f32(v1.y));
   }
 }
 
@@ -728,7 +735,7 @@ int hlbl_f32_tile_copy(hlbl_ctx* c, const double* d_block, float* d_out) {
     if (e != cudaSuccess) return cuda_fail(e, "wait for staged block");
     c->stage_pending = false;
   }
-  f32_tile_copy_kernel<<<c->nsm * 8, 256, 0, c->stream>>>(d_block, c->geo, d_out);
+  f32_tile_copy_kernel<<<dim3(std::max(1, c->nsm * 8 / 24), 24), 256, 0, c->stream>>>(d_block, c->geo, d_out);
   return check_launch("hlbl_f32_tile_copy launch");
 }
 
