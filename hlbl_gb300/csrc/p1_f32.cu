@@ -38,67 +38,88 @@ template <int NFL> __host__ __device__ constexpr int threads() { return 144 * NF
 template <int ST, int NFL> __host__ __device__ constexpr int min_ctas() { return NFL == 1 ? 3 : (ST == 1 ? 2 : 1); }
 
 // One tile's contribution of thread (fl, ia, ib): per site the eight
-// spin-block products, X_sigma, and the zerohalf-weighted sums, summed over
-// the tile in FP32 and added into the Kahan accumulators.
+// spin-block products and X_sigma; added into the Kahan accumulators.
+// The zerohalf weights zh_0..zh_2 are constant along a run of sites of
+// fixed (t, x, y) (z fastest), so per site only the run sums S_g = sum X_g and
+// T_g = sum zh_3 X_g are formed, and at the end of a run
+//   dzu[(r,g)] += zh_r S_g - zh_g S_r  (g < 3),   zh_r S_3 - T_r  (g = 3),
+//   dzsu[g]    += S_g.
+// z0: the tile's first site's local z, LZ: the local extent in z.
 __device__ __forceinline__ void tile_sums(const float* __restrict__ Arow, const float* __restrict__ Brow,
-                                          const float (*zhs)[4], int nvalid, KahanF (&acc_u)[6][2],
-                                          KahanF (&acc_s)[4][2]) {
-    float tu[6][2], ts[4][2];
+                                          const float (*zhs)[4], int nvalid, int z0, int LZ,
+                                          KahanF (&acc_u)[6][2], KahanF (&acc_s)[4][2]) {
+  float tu[6][2], ts[4][2], S[4][2], T[4][2];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) tu[k][0] = tu[k][1] = 0.f;
+  for (int k = 0; k < 6; ++k) tu[k][0] = tu[k][1] = 0.f;
 #pragma unroll
-    for (int s = 0; s < 4; ++s) ts[s][0] = ts[s][1] = 0.f;
-#pragma unroll 1
-    for (int s = 0; s < nvalid; ++s) {
-      float A[24], B[24];
+  for (int g = 0; g < 4; ++g) ts[g][0] = ts[g][1] = S[g][0] = S[g][1] = T[g][0] = T[g][1] = 0.f;
+  auto flush = [&](const float* zh) {
 #pragma unroll
-      for (int c4 = 0; c4 < 6; ++c4) {
-        float4 const a = *reinterpret_cast<const float4*>(Arow + c4 * 64 + s * 4);
-        float4 const b = *reinterpret_cast<const float4*>(Brow + c4 * 64 + s * 4);
-        A[4 * c4] = a.x; A[4 * c4 + 1] = a.y; A[4 * c4 + 2] = a.z; A[4 * c4 + 3] = a.w;
-        B[4 * c4] = b.x; B[4 * c4 + 1] = b.y; B[4 * c4 + 2] = b.z; B[4 * c4 + 3] = b.w;
-      }
-      // P[s1][s2] = sum_c conj(B[s1][c]) A[s2][c] for s2 = s1^2 and 3-s1
-      float pa[4][2], pb[4][2];
+    for (int k = 0; k < 6; ++k) {
+      int const r = comb_rho(k), g = comb_sigma(k);
 #pragma unroll
-      for (int s1 = 0; s1 < 4; ++s1) {
-        float ar = 0, ai = 0, br = 0, bi = 0;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          float const yr = B[2 * (3 * s1 + c)], yi = B[2 * (3 * s1 + c) + 1];
-          int const sa = 2 * (3 * (s1 ^ 2) + c), sb = 2 * (3 * (3 - s1) + c);
-          ar += yr * A[sa] + yi * A[sa + 1];  ai += yr * A[sa + 1] - yi * A[sa];
-          br += yr * A[sb] + yi * A[sb + 1];  bi += yr * A[sb + 1] - yi * A[sb];
-        }
-        pa[s1][0] = ar; pa[s1][1] = ai; pb[s1][0] = br; pb[s1][1] = bi;
-      }
-      float X[4][2];
-#pragma unroll
-      for (int sg = 0; sg < 4; ++sg) {
-        float xr = 0, xi = 0;
-#pragma unroll
-        for (int s1 = 0; s1 < 4; ++s1) {
-          float const* pp = (sg == 0 || sg == 3) ? pa[s1] : pb[s1];
-          float vr, vi;
-          mul_iph(g5g_ph(sg, s1), pp[0], pp[1], vr, vi);
-          xr += vr; xi += vi;
-        }
-        X[sg][0] = xr; X[sg][1] = xi;
-      }
-#pragma unroll
-      for (int sg = 0; sg < 4; ++sg) { ts[sg][0] += X[sg][0]; ts[sg][1] += X[sg][1]; }
-      const float* zh = zhs[s];
-#pragma unroll
-      for (int k = 0; k < 6; ++k) {
-        int const r = comb_rho(k), g = comb_sigma(k);
-        tu[k][0] += zh[r] * X[g][0] - zh[g] * X[r][0];
-        tu[k][1] += zh[r] * X[g][1] - zh[g] * X[r][1];
-      }
+      for (int c = 0; c < 2; ++c)
+        tu[k][c] += g == 3 ? zh[r] * S[3][c] - T[r][c] : zh[r] * S[g][c] - zh[g] * S[r][c];
     }
 #pragma unroll
-    for (int k = 0; k < 6; ++k) { acc_u[k][0].add(tu[k][0]); acc_u[k][1].add(tu[k][1]); }
+    for (int g = 0; g < 4; ++g) {
 #pragma unroll
-    for (int s = 0; s < 4; ++s) { acc_s[s][0].add(ts[s][0]); acc_s[s][1].add(ts[s][1]); }
+      for (int c = 0; c < 2; ++c) {
+        ts[g][c] += S[g][c];
+        S[g][c] = T[g][c] = 0.f;
+      }
+    }
+  };
+  int z = z0;
+#pragma unroll 1
+  for (int s = 0; s < nvalid; ++s) {
+    if (z == LZ) {  // a new run starts at this site
+      flush(zhs[s - 1]);
+      z = 0;
+    }
+    ++z;
+    float A[24], B[24];
+#pragma unroll
+    for (int c4 = 0; c4 < 6; ++c4) {
+      float4 const a = *reinterpret_cast<const float4*>(Arow + c4 * 64 + s * 4);
+      float4 const b = *reinterpret_cast<const float4*>(Brow + c4 * 64 + s * 4);
+      A[4 * c4] = a.x; A[4 * c4 + 1] = a.y; A[4 * c4 + 2] = a.z; A[4 * c4 + 3] = a.w;
+      B[4 * c4] = b.x; B[4 * c4 + 1] = b.y; B[4 * c4 + 2] = b.z; B[4 * c4 + 3] = b.w;
+    }
+    // P[s1][s2] = sum_c conj(B[s1][c]) A[s2][c] for s2 = s1^2 and 3-s1
+    float pa[4][2], pb[4][2];
+#pragma unroll
+    for (int s1 = 0; s1 < 4; ++s1) {
+      float ar = 0, ai = 0, br = 0, bi = 0;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float const yr = B[2 * (3 * s1 + c)], yi = B[2 * (3 * s1 + c) + 1];
+        int const sa = 2 * (3 * (s1 ^ 2) + c), sb = 2 * (3 * (3 - s1) + c);
+        ar += yr * A[sa] + yi * A[sa + 1];  ai += yr * A[sa + 1] - yi * A[sa];
+        br += yr * A[sb] + yi * A[sb + 1];  bi += yr * A[sb + 1] - yi * A[sb];
+      }
+      pa[s1][0] = ar; pa[s1][1] = ai; pb[s1][0] = br; pb[s1][1] = bi;
+    }
+    float const z3 = zhs[s][3];
+#pragma unroll
+    for (int sg = 0; sg < 4; ++sg) {
+      float xr = 0, xi = 0;
+#pragma unroll
+      for (int s1 = 0; s1 < 4; ++s1) {
+        float const* pp = (sg == 0 || sg == 3) ? pa[s1] : pb[s1];
+        float vr, vi;
+        mul_iph(g5g_ph(sg, s1), pp[0], pp[1], vr, vi);
+        xr += vr; xi += vi;
+      }
+      S[sg][0] += xr; S[sg][1] += xi;
+      T[sg][0] = fmaf(z3, xr, T[sg][0]); T[sg][1] = fmaf(z3, xi, T[sg][1]);
+    }
+  }
+  if (nvalid > 0) flush(zhs[nvalid - 1]);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) { acc_u[k][0].add(tu[k][0]); acc_u[k][1].add(tu[k][1]); }
+#pragma unroll
+  for (int g = 0; g < 4; ++g) { acc_s[g][0].add(ts[g][0]); acc_s[g][1].add(ts[g][1]); }
 }
 
 template <int ST, int NFL>
@@ -170,7 +191,7 @@ p1f32_kernel(TcBatch tb, Geometry geo, double* __restrict__ partials, int* __res
     if (!mbar_wait(&s_bar[st], parity)) s_fail = 1;
     __syncthreads();
     if (s_fail) break;
-    tile_sums(Arow, Brow, sm.zh, nvalid, acc_u, acc_s);
+    tile_sums(Arow, Brow, sm.zh, nvalid, (int)(s0 % geo.local[3]), geo.local[3], acc_u, acc_s);
     __syncthreads();  // the stage and zh are rewritten for the next tile
     if (ST == 1 && t == 0 && tile + gridDim.x < ntiles) {
       fence_proxy_async_smem();
@@ -292,8 +313,10 @@ p1f32_ws_kernel(TcBatch tb, Geometry geo, double* __restrict__ partials, int* __
       }
       if (*fail) break;
       if (t < 144) {
-        int const nvalid = (int)min((long long)kTS, geo.V - tile * kTS);
-        tile_sums(sm.stage[st][ia], sm.stage[st][12 + ib], sm.zh[st], nvalid, acc_u, acc_s);
+        long long const s0 = tile * kTS;
+        int const nvalid = (int)min((long long)kTS, geo.V - s0);
+        tile_sums(sm.stage[st][ia], sm.stage[st][12 + ib], sm.zh[st], nvalid, (int)(s0 % geo.local[3]),
+                  geo.local[3], acc_u, acc_s);
       }
       __syncwarp();
       if (lane == 0) mbar_arrive_local(&s_empty[st]);
