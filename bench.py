@@ -492,14 +492,30 @@ def main():
     # same work have measured 45 and 130 pairs/s in one run), so the median
     # is reported and all five are listed
     e2e_pass()
-    e2e_runs = []
+    # a 1 GB pinned host -> device copy just before each pass: the host link's
+    # bandwidth at that moment (the machine's host side is shared)
+    probe_h = torch.empty(1 << 30, dtype=torch.uint8, pin_memory=True)
+    probe_d = torch.empty(1 << 30, dtype=torch.uint8, device="cuda")
+
+    def h2d_probe():
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            probe_d.copy_(probe_h, non_blocking=True)
+            e1.record(stream)
+        e1.synchronize()
+        return (1 << 30) / (e0.elapsed_time(e1) * 1e-3) / 1e9
+
+    e2e_runs, h2d_gbs = [], []
     for _ in range(5):
+        h2d_gbs.append(round(h2d_probe(), 1))
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
         h2d, d2h = e2e_pass()
         e2e_runs.append(time.perf_counter() - t0)
+    del probe_h, probe_d
     e2e_s = statistics.median(e2e_runs)
     if dist:
         t = torch.tensor([e2e_s], device="cuda")
@@ -595,6 +611,7 @@ def main():
                 "h2d_bytes_per_step": int(h2d / max(1, len(timed))),
                 "d2h_bytes_per_step": int(d2h / max(1, len(timed))),
                 "passes_pairs_per_s": [round(pairs_total / t, 2) for t in e2e_runs],
+                "h2d_probe_gbs_before_each_pass": h2d_gbs,
                 "how": "median of five passes over the timed steps after one untimed pass; each "
                        "step stages its new block from pinned host memory on the side stream while "
                        "the previous step computes"},

@@ -561,9 +561,9 @@ static __global__ void qed_weights_exact_kernel(Geometry geo, WArgs args, double
 // FP32 keeps a few 1e-7 relative accuracy; qed_f32.cuh), in FP64 inside that
 // radius (near the origin) -- the FP64 QED evaluation is kept only there.
 // One thread per site: its three evaluations share the site's coordinates
-// (32-bit integer arithmetic, V < 2^31); the invariants are FP64 as in the
-// FP64 weight, the quadrature FP32; the FP64 evaluations near the origin are
-// shared by the warp (one node per lane) instead of run by single lanes.
+// (32-bit integer arithmetic, V < 2^31); the quadrature is FP32; the FP64
+// evaluations near the origin are shared by the warp (one node per lane)
+// instead of run by single lanes.
 static __global__ void qed_weights_fp32_kernel(Geometry geo, WArgs args, double r64, QedF32 qf,
                                                double* __restrict__ w) {
   int const pi = blockIdx.y;
@@ -571,6 +571,13 @@ static __global__ void qed_weights_fp32_kernel(Geometry geo, WArgs args, double 
   int const yv[4] = {args.batch.p[pi].yv[0], args.batch.p[pi].yv[1], args.batch.p[pi].yv[2], args.batch.p[pi].yv[3]};
   w += (size_t)pi * geo.V * 3 * HLBL_QED_NW;
   unsigned const V = (unsigned)geo.V, stride = gridDim.x * blockDim.x;
+  float const xuf = (float)args.xunit, r64f = (float)r64;
+  int iy[4], ny = 0;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    iy[r] = coord_map(mod_pos(yv[r], geo.global[r]), geo.global[r]);
+    ny += iy[r] * iy[r];
+  }
   // every lane runs every iteration (the near-origin evaluations are shared
   // by the warp); lanes past the end compute on the last site and store nothing
   for (unsigned base = blockIdx.x * blockDim.x; base < V; base += stride) {
@@ -582,33 +589,48 @@ static __global__ void qed_weights_fp32_kernel(Geometry geo, WArgs args, double 
     c[2] = (int)(s % (unsigned)geo.local[2]); s /= (unsigned)geo.local[2];
     c[1] = (int)(s % (unsigned)geo.local[1]); s /= (unsigned)geo.local[1];
     c[0] = (int)s;
-    // the arguments in FP64 (small integers times xunit) and their
-    // invariants |a|, cos(a, b), |b| in FP64, as the FP64 weight has them
-    double xm[4], xmy[4];
+    // the arguments are small integer vectors times xunit: |a|^2, |b|^2 and
+    // a.b are exact integer sums (times xunit^2), so |a|, |b| and cos(a, b)
+    // come out of correctly rounded FP32 square roots and one division
+    // (within 1.5 ulp; the FP64 weight gets the same invariants in FP64)
+    int ix[4], ixy[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       int const G = geo.global[r];
       int const rel = (c[r] + geo.pc[r] * geo.local[r] - gsx[r] + G) % G;
-      xm[r] = coord_map(rel, G) * args.xunit;
-      xmy[r] = coord_map_diff(rel, yv[r], G) * args.xunit;
+      ix[r] = coord_map(rel, G);
+      ixy[r] = coord_map_diff(rel, yv[r], G);
     }
-    double ymd[4];
+    int nx = 0, nxy = 0, dxy = 0, dxx = 0;
 #pragma unroll
-    for (int r = 0; r < 4; ++r) ymd[r] = coord_map(mod_pos(yv[r], geo.global[r]), geo.global[r]) * args.xunit;
+    for (int r = 0; r < 4; ++r) {
+      nx += ix[r] * ix[r];
+      nxy += ixy[r] * ixy[r];
+      dxy += ix[r] * iy[r];
+      dxx += ix[r] * ixy[r];
+    }
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
       // e = 0: K(xm, ym), e = 1: K(ym, xm), e = 2: K(xm, x - y)
-      const double* a = e == 1 ? ymd : xm;
-      const double* b = e == 0 ? ymd : (e == 1 ? xm : xmy);
-      double Xd, cd, Yd;
-      hlbl_qed_invariants(a, b, &Xd, &cd, &Yd);
-      bool const near = fmin(Xd, Yd) < r64;
+      int const na = e == 1 ? ny : nx, nb = e == 0 ? ny : (e == 1 ? nx : nxy), nab = e == 2 ? dxx : dxy;
+      float const ra = sqrtf((float)na), rb = sqrtf((float)nb);
+      float const X = xuf * ra, Y = xuf * rb;
+      float cc = (na > 0 && nb > 0) ? (float)nab / (ra * rb) : 0.f;
+      cc = fminf(1.f, fmaxf(-1.f, cc));
+      bool const near = fminf(X, Y) < r64f;
       double ww[HLBL_QED_NW];
       {
         float wf[HLBL_QED_NW];
-        weights_f32<false, false>(qf, (float)Xd, (float)cd, (float)Yd, wf);
+        weights_f32<false, false>(qf, X, cc, Y, wf);
 #pragma unroll
         for (int j = 0; j < HLBL_QED_NW; ++j) ww[j] = (double)wf[j];
+      }
+      double Xd = 0, cd = 0, Yd = 0;
+      if (near) {
+        Xd = args.xunit * sqrt((double)na);
+        Yd = args.xunit * sqrt((double)nb);
+        cd = (na > 0 && nb > 0) ? (double)nab / sqrt((double)na * (double)nb) : 0.0;
+        cd = cd > 1.0 ? 1.0 : (cd < -1.0 ? -1.0 : cd);
       }
       // near the origin: the FP64 weight of the FP64 arguments, the warp
       // sharing each such evaluation (one quadrature node per lane)
