@@ -38,7 +38,7 @@ def test_random_provider_seed_folding():
 def test_kernel_sum_matches_reference(case):
     src, y = S.case_inputs(case)
     got = S.oracle_kernel_sum(src, y, case["gsx"], case["yv"], case["xunit"], case["lattice"])
-    # 1e-12 relative per pair and flavour (the spec bar for the FP64 path)
+    # 1e-12 relative per pair and flavour (the FP64 path's bar)
     assert S.rel_err(got, case["kernel_sum"]) <= 1e-12
 
 
