@@ -16,6 +16,7 @@ any object with the same two methods).
 """
 from __future__ import annotations
 
+import time
 from dataclasses import dataclass, field
 from typing import Callable, List, Tuple
 
@@ -59,12 +60,16 @@ class RunStats:
 
 def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cache: PropagatorCache,
               chain: int = 0, precision=0, batched: bool = False, graphs: bool = False,
-              out_factory=None, sources_2p2=None, results_2p2=None, at_2p2=None):
+              out_factory=None, sources_2p2=None, results_2p2=None, at_2p2=None, writer=None,
+              timing=None):
     """One chain; returns ([PairResult], RunStats). With batched=True,
     out_factory(n) must return a device buffer of n x 2 doubles. 2+2: either
     `sources_2p2` ({global site: targets}, at the site's first solve in this
     chain) or `at_2p2` ({solve position as in the schedule: targets}, a
-    plan over several chains, run_chains); results appended to `results_2p2`."""
+    plan over several chains, run_chains); results appended to `results_2p2`.
+    `writer` (output.ResultWriter) gets each window's rows and 2+2 results,
+    `timing` (output.TimingLog) a row per solve, kernel sum (the per-pair
+    loop) and 2+2 source (driver.cpp:58-151)."""
     pending = {}
     for older, newer, _ in sch.all_pairs(steps):
         pending[older] = pending.get(older, 0) + 1
@@ -78,20 +83,30 @@ def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cach
     if (todo_2p2 or at) and results_2p2 is None:
         raise ValueError("run_chain: 2+2 sources need a results_2p2 list")
 
+    window_2p2 = []
+
     def solve(window, position):
         dest = cache.begin_insert(position)
         site = tuple(wrap(position))
+        t0 = time.perf_counter()
         provider(site, dest)
+        if timing is not None:
+            timing.solve(chain, window, site, time.perf_counter() - t0, 0)
         stats.positions_solved += 1
         # 2+2 at the site's first solve, from the block just solved
         targets = at.pop(tuple(position), None)
         if targets is None:
             targets = todo_2p2.pop(site, None)
         if targets is not None:
+            t0 = time.perf_counter()
             pc = contractor.pieces_2p2(dest, site, targets, xunit, precision)
-            results_2p2.append(Result2p2(site, [tuple(t) for t in targets],
-                                         [tuple(sch.site_map_diff(t, site, lattice)) for t in targets],
-                                         chain, window, pc.p1, pc.p234))
+            if timing is not None:
+                timing.pieces_2p2(chain, window, site, time.perf_counter() - t0)
+            r = Result2p2(site, [tuple(t) for t in targets],
+                          [tuple(sch.site_map_diff(t, site, lattice)) for t in targets],
+                          chain, window, pc.p1, pc.p234)
+            results_2p2.append(r)
+            window_2p2.append(r)
             stats.pieces_2p2 += 1
             stats.targets_2p2 += len(targets)
         cache.end_insert(position)
@@ -112,7 +127,10 @@ def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cach
                     d_x = cache.device_ptr(q, 1)
                     gx = wrap(q)
                     yv = sch.site_map_diff(src.position, q, lattice)
+                    t0 = time.perf_counter()
                     ks = contractor.kernel_sum(d_x, d_y, gx, yv, xunit, precision)
+                    if timing is not None:
+                        timing.kernel_sum(chain, st.index, gx, gy, time.perf_counter() - t0)
                     window_rows.append(PairResult(gx, gy, yv, chain, st.index, tuple(ks)))
                     cache.pair_done(q, src.position)
                     stats.pairs += 1
@@ -152,6 +170,12 @@ def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cach
                 g.close()
         results.extend(window_rows)
         stats.windows.append(len(window_rows))
+        # the window's rows go to the result file as the window ends (driver.cpp:136-151)
+        if writer is not None:
+            writer.append(window_rows)
+            if window_2p2:
+                writer.append_2p2(window_2p2)
+        window_2p2.clear()
     if cache.size() != 0:
         raise RuntimeError("run_chain: propagators left in the cache")
     stats.cache_peak = cache.peak
@@ -160,7 +184,7 @@ def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cach
 
 def run_chains(chains, lattice, xunit: float, provider: Callable, contractor, cache: PropagatorCache,
                precision=0, batched: bool = False, graphs: bool = False, out_factory=None,
-               sources_2p2=None, results_2p2=None):
+               sources_2p2=None, results_2p2=None, writer=None, timing=None):
     """Several chains over one cache (driver.cpp:169-208): the chains in
     order, the 2+2 of each source in `sources_2p2` ([(source, targets)]) at
     its first solve over all chains (schedule.plan_2p2). Returns
@@ -177,7 +201,8 @@ def run_chains(chains, lattice, xunit: float, provider: Callable, contractor, ca
         at = {pos: list(sources_2p2[i][1]) for pos, i in plan.at[c].items()}
         res, st = run_chain(steps, lattice, xunit, provider, contractor, cache, chain=c,
                             precision=precision, batched=batched, graphs=graphs,
-                            out_factory=out_factory, results_2p2=results_2p2, at_2p2=at)
+                            out_factory=out_factory, results_2p2=results_2p2, at_2p2=at,
+                            writer=writer, timing=timing)
         results.extend(res)
         total.positions_solved += st.positions_solved
         total.pairs += st.pairs
