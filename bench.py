@@ -17,7 +17,7 @@ Printed (one JSON line, rank 0):
   fp64       pairs/s of the plain FP64 path on the same pairs;
   e2e        the same metric through the C ABI with host buffers: each step
              copies its new block from pinned host memory and reads back its
-             kernel sums (median of five passes);
+             kernel sums (median of seven passes);
   roofline   the dominant kernel (pass 2, against a cuBLAS TF32 GEMM measured
              in the run; pass 1 against the measured HBM bandwidth beside it);
   pieces_2p2 the 2+2 pieces of one source for 16 targets (compute_2p2_gpu);
@@ -483,14 +483,16 @@ def main():
                 host_out[k:k + len(xs)].copy_(res[k:k + len(xs)], non_blocking=True)
             d2h += len(xs) * 16
             k += len(xs)
+        enq = time.perf_counter()
         stream.synchronize()
-        return h2d, d2h
+        return h2d, d2h, enq
 
     # one untimed pass first (the first copies from freshly pinned pages and
     # the first launches of this call sequence are not representative), then
-    # five timed passes: the host side of the box is shared (passes of the
-    # same work have measured 45 and 130 pairs/s in one run), so the median
-    # is reported and all five are listed
+    # seven timed passes: the host side of the box is shared (passes of the
+    # same work have measured 45 and 139 pairs/s in one run), so the median
+    # is reported and all seven are listed, each with the host time spent
+    # enqueueing it (a slow pass with a short enqueue time waited on the device)
     e2e_pass()
     # a 1 GB pinned host -> device copy just before each pass: the host link's
     # bandwidth at that moment (the machine's host side is shared)
@@ -506,15 +508,16 @@ def main():
         e1.synchronize()
         return (1 << 30) / (e0.elapsed_time(e1) * 1e-3) / 1e9
 
-    e2e_runs, h2d_gbs = [], []
-    for _ in range(5):
+    e2e_runs, e2e_enq, h2d_gbs = [], [], []
+    for _ in range(7):
         h2d_gbs.append(round(h2d_probe(), 1))
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
-        h2d, d2h = e2e_pass()
+        h2d, d2h, enq = e2e_pass()
         e2e_runs.append(time.perf_counter() - t0)
+        e2e_enq.append(enq - t0)
     del probe_h, probe_d
     e2e_s = statistics.median(e2e_runs)
     if dist:
@@ -611,8 +614,9 @@ def main():
                 "h2d_bytes_per_step": int(h2d / max(1, len(timed))),
                 "d2h_bytes_per_step": int(d2h / max(1, len(timed))),
                 "passes_pairs_per_s": [round(pairs_total / t, 2) for t in e2e_runs],
+                "passes_enqueue_ms": [round(1e3 * t, 1) for t in e2e_enq],
                 "h2d_probe_gbs_before_each_pass": h2d_gbs,
-                "how": "median of five passes over the timed steps after one untimed pass; each "
+                "how": "median of seven passes over the timed steps after one untimed pass; each "
                        "step stages its new block from pinned host memory on the side stream while "
                        "the previous step computes"},
         "roofline": dominant,
