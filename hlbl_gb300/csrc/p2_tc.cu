@@ -100,6 +100,14 @@ __device__ __forceinline__ uint32_t tf32_rna(float x) {
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
   return r;
 }
+// The same rounding (to nearest, ties away from zero, the low 13 bits
+// cleared) on the integer pipe, for finite x: adding half a TF32 unit to the
+// magnitude bits carries into the kept bits exactly when the dropped part is
+// at least half; a carry into the exponent is the correct round-up. The
+// D-formation warps round 16 values per (p, q) pair this way.
+__device__ __forceinline__ float tf32_round(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
 __device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -377,41 +385,53 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
     }
   } else if (warp == kWarpMma) {
     // ---- MMA issue ----------------------------------------------------------------
+    // The tensor pipe runs the six MMAs of a chunk in about 500 cycles, so the
+    // issuing thread's own per-chunk work has to stay well below that: the
+    // stage descriptors differ only in their start address (bits 0-13, in
+    // 16-byte units, no carry below 256 KB), so they are formed once and
+    // advanced by constants; ring positions and phases are counters.
     if (lane == 0) {
-      int ac = 0, bc = 0;
+      uint64_t const a_desc0 = sdesc(smem_u32(sm.A[0][0]), (kM / 8) * 128, 128);
+      uint64_t const b_desc0 = sdesc(smem_u32(sm.B[0][0]), (kBtN / 8) * 128, 128);
+      // in 16-byte units: stage to stage, hi to lo part, k-step to k-step
+      // (two core columns: 2*16*128 and 2*20*128 bytes)
+      constexpr uint64_t kAStage16 = 2 * kAPart * 4 / 16, kALo16 = kAPart * 4 / 16, kAK16 = 2 * (kM / 8) * 128 / 16;
+      constexpr uint64_t kBStage16 = 2 * kBPart * 4 / 16, kBLo16 = kBPart * 4 / 16, kBK16 = 2 * (kBtN / 8) * 128 / 16;
+      int as = 0, bs = 0;
+      uint32_t aph = 0, bph = 0;
+      uint32_t const dc = tmem + kCorrCol;
       bool ok = true;
       for (int P = 0; ok && P < nph; ++P) {
         // first half into main buffer P&1 (phase P-1's second half, free once
         // folded), second half into buffer (P+1)&1 (free once dotted)
         if (!wait_or_fail(&sm.folded, (uint32_t)((P & 1) ^ 1), fail)) break;
         tc_fence_after();
-        uint32_t const dc = tmem + kCorrCol;
-        for (int c = 0; c < kChunks; ++c, ++ac, ++bc) {
+        uint32_t const d0 = tmem + (uint32_t)((P & 1) * kBtN), d1 = tmem + (uint32_t)(((P + 1) & 1) * kBtN);
+        for (int c = 0; c < kChunks; ++c) {
           if (c == kHalf) {
             if (!wait_or_fail(&sm.dotted, (uint32_t)((P & 1) ^ 1), fail)) { ok = false; break; }
             tc_fence_after();
           }
-          uint32_t const d = tmem + (uint32_t)(((c < kHalf ? P : P + 1) & 1) * kBtN);
-          int const as = ac % kAStages, bs = bc % kBStages;
-          if (!wait_or_fail(&sm.a_full[as], (uint32_t)((ac / kAStages) & 1), fail) ||
-              !wait_or_fail(&sm.b_full[bs], (uint32_t)((bc / kBStages) & 1), fail)) { ok = false; break; }
-          tc_fence_after();
-          uint32_t const a0 = smem_u32(sm.A[as][0]), b0 = smem_u32(sm.B[bs][0]);
-#pragma unroll
-          for (int ks = 0; ks < 2; ++ks) {
-            // hi.hi into the main buffer, hi.lo and lo.hi into the correction
-            // accumulator; parts are kAPart*4 / kBPart*4 bytes apart, k-steps
-            // 2 core columns (2*16*128 / 2*20*128 bytes) apart
-            uint32_t const ak = a0 + ks * 2 * (kM / 8) * 128, bk = b0 + ks * 2 * (kBtN / 8) * 128;
-            uint64_t const ahi = sdesc(ak, (kM / 8) * 128, 128), alo = sdesc(ak + kAPart * 4, (kM / 8) * 128, 128);
-            uint64_t const bhi = sdesc(bk, (kBtN / 8) * 128, 128), blo = sdesc(bk + kBPart * 4, (kBtN / 8) * 128, 128);
-            mma_tf32(d, ahi, bhi, ((c % kHalf) | ks) ? 1u : 0u);
-            mma_tf32(dc, ahi, blo, (c | ks) ? 1u : 0u);
-            mma_tf32(dc, alo, bhi, 1u);
+          if (!wait_or_fail(&sm.a_full[as], aph, fail) || !wait_or_fail(&sm.b_full[bs], bph, fail)) {
+            ok = false;
+            break;
           }
+          tc_fence_after();
+          uint32_t const d = c < kHalf ? d0 : d1;
+          uint64_t const ahi = a_desc0 + (uint64_t)as * kAStage16, bhi = b_desc0 + (uint64_t)bs * kBStage16;
+          // hi.hi into the main buffer, hi.lo and lo.hi into the correction
+          // accumulator; two k-steps of 8
+          mma_tf32(d, ahi, bhi, (c != 0 && c != kHalf) ? 1u : 0u);
+          mma_tf32(dc, ahi, bhi + kBLo16, c ? 1u : 0u);
+          mma_tf32(dc, ahi + kALo16, bhi, 1u);
+          mma_tf32(d, ahi + kAK16, bhi + kBK16, 1u);
+          mma_tf32(dc, ahi + kAK16, bhi + kBK16 + kBLo16, 1u);
+          mma_tf32(dc, ahi + kAK16 + kALo16, bhi + kBK16, 1u);
           mma_any = true;
           mma_commit(&sm.a_empty[as]);
           mma_commit(&sm.b_empty[bs]);
+          if (++as == kAStages) { as = 0; aph ^= 1u; }
+          if (++bs == kBStages) { bs = 0; bph ^= 1u; }
         }
         if (!ok) break;
         mma_commit(&sm.acc_full);
@@ -489,10 +509,10 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
 #pragma unroll
           for (int mu = 0; mu < 4; ++mu) {
             float4 hi, lo;
-            hi.x = __uint_as_float(tf32_rna(d[mu][0])); hi.y = __uint_as_float(tf32_rna(d[mu][1]));
-            hi.z = __uint_as_float(tf32_rna(d[mu][2])); hi.w = __uint_as_float(tf32_rna(d[mu][3]));
-            lo.x = __uint_as_float(tf32_rna(d[mu][0] - hi.x)); lo.y = __uint_as_float(tf32_rna(d[mu][1] - hi.y));
-            lo.z = __uint_as_float(tf32_rna(d[mu][2] - hi.z)); lo.w = __uint_as_float(tf32_rna(d[mu][3] - hi.w));
+            hi.x = tf32_round(d[mu][0]); hi.y = tf32_round(d[mu][1]);
+            hi.z = tf32_round(d[mu][2]); hi.w = tf32_round(d[mu][3]);
+            lo.x = tf32_round(d[mu][0] - hi.x); lo.y = tf32_round(d[mu][1] - hi.y);
+            lo.z = tf32_round(d[mu][2] - hi.z); lo.w = tf32_round(d[mu][3] - hi.w);
             *reinterpret_cast<float4*>(Ahi + mu * 4 * 32) = hi;
             *reinterpret_cast<float4*>(Alo + mu * 4 * 32) = lo;
           }
