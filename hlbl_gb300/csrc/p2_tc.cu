@@ -33,8 +33,9 @@
 // dot. The two main buffers swap roles every phase: the next phase's first
 // half only waits for that fold, its second half for the dot.
 // Pipelines (mbarriers; every wait bounded, kWaitLimit polls):
-//   rows -> D warps (S double buffer per phase, Y ring of 4 rows),
-//   D warps -> MMA (A ring of 3), B producer -> MMA (B ring of 4),
+//   rows -> D warps (S double buffer per phase, Y ring of 3 rows),
+//   D warps -> MMA (A ring of 4), B producer -> MMA (B ring of 4), one
+//   commit per chunk frees both stages,
 //   MMA -> epilogue (acc_full), epilogue -> MMA (folded, dotted).
 //
 // Inputs are the FP32 tile copies pass 1 writes while it converts each
@@ -58,7 +59,12 @@ constexpr int kSites = 32;                 // sites per tile
 constexpr int kM = 128;                    // MMA rows: (mu, site)
 constexpr int kKc = 16;                    // K per chunk
 constexpr int kChunks = kBtK / kKc;        // 18
-constexpr int kAStages = 3, kBStages = 4, kYSlots = 4;
+// A and B rings of the same depth, released by one commit per chunk: the
+// tensor pipe's completion reaches the waiting producers about 2,500 cycles
+// after a chunk is issued, so four chunks (about 2,400 cycles of MMAs) must
+// be in flight to keep it busy; three Y rows cover the 16 (p, q) of two
+// chunks in flight per D group
+constexpr int kStages = 4, kAStages = kStages, kBStages = kStages, kYSlots = 3;
 constexpr int kHalf = kChunks / 2;               // chunks per main-accumulator half
 constexpr uint32_t kCorrCol = 2 * kBtN;          // the correction accumulator's first column
 constexpr int kAPart = kM * kKc;           // floats per A part (hi or lo)
@@ -81,12 +87,13 @@ struct __align__(1024) Smem {
   float A[kAStages][2][kAPart];
   float B[kBStages][2][kBPart];
   uint64_t s_full[2], s_empty[2], y_full[kYSlots], y_empty[kYSlots];
-  uint64_t a_full[kAStages], a_empty[kAStages], b_full[kBStages], b_empty[kBStages];
+  uint64_t a_full[kStages], b_full[kStages], empty[kStages];
   uint64_t acc_full, folded, dotted, mma_done;
   uint32_t taddr;
   int fail;
   double red[kEWarps][2][2];
 };
+static_assert(sizeof(Smem) <= 232448, "pass-2 shared memory above the 227 KB a CTA may have");
 
 // ---- tcgen05 / TMA helpers ---------------------------------------------------
 // shared-memory matrix descriptor, no swizzle: start, leading byte offset
@@ -311,8 +318,11 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
   if (t == 0) {
     for (int i = 0; i < 2; ++i) { mbar_init(&sm.s_full[i], 1); mbar_init(&sm.s_empty[i], kDWarps); }
     for (int i = 0; i < kYSlots; ++i) { mbar_init(&sm.y_full[i], 1); mbar_init(&sm.y_empty[i], kDWarps); }
-    for (int i = 0; i < kAStages; ++i) { mbar_init(&sm.a_full[i], kDGroup); mbar_init(&sm.a_empty[i], 1); }
-    for (int i = 0; i < kBStages; ++i) { mbar_init(&sm.b_full[i], 1); mbar_init(&sm.b_empty[i], 1); }
+    for (int i = 0; i < kStages; ++i) {
+      mbar_init(&sm.a_full[i], kDGroup);
+      mbar_init(&sm.b_full[i], 1);
+      mbar_init(&sm.empty[i], 1);
+    }
     mbar_init(&sm.acc_full, 1);
     mbar_init(&sm.folded, kEWarps);
     mbar_init(&sm.dotted, kEWarps);
@@ -360,8 +370,8 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
           bulk_g2s(sm.Y[slot], row_ptr(y32, f, p, tile), kRowBytes, &sm.y_full[slot]);
           rows_issued_y = uy;
           // the next phase's S rows into the other buffer, once its readers
-          // (the previous phase) are done: issuing Y[4] needed Y[0] of this
-          // phase consumed, so that wait no longer blocks the Y rows
+          // (the previous phase) are done: issuing row kYSlots needed row 0
+          // of this phase consumed, so that wait no longer blocks the Y rows
           if (p == kYSlots && P + 1 < nph) ok = issue_S(P + 1);
         }
       }
@@ -375,7 +385,7 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
         const float* src = btu + ((size_t)pi * 2 + (P & 1)) * kChunks * 2 * kBPart;
         for (int c = 0; c < kChunks; ++c, ++bc) {
           int const st = bc % kBStages;
-          if (!wait_or_fail(&sm.b_empty[st], (uint32_t)(((bc / kBStages) & 1) ^ 1), fail)) { ok = false; break; }
+          if (!wait_or_fail(&sm.empty[st], (uint32_t)(((bc / kBStages) & 1) ^ 1), fail)) { ok = false; break; }
           fence_proxy_async_smem();
           mbar_arrive_expect_tx(&sm.b_full[st], 2 * kBPart * 4);
           bulk_g2s(sm.B[st][0], src + (size_t)c * 2 * kBPart, 2 * kBPart * 4, &sm.b_full[st]);
@@ -428,8 +438,7 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
           mma_tf32(dc, ahi + kAK16, bhi + kBK16 + kBLo16, 1u);
           mma_tf32(dc, ahi + kAK16 + kALo16, bhi + kBK16, 1u);
           mma_any = true;
-          mma_commit(&sm.a_empty[as]);
-          mma_commit(&sm.b_empty[bs]);
+          mma_commit(&sm.empty[as]);  // frees A and B stage as (= bs)
           if (++as == kAStages) { as = 0; aph ^= 1u; }
           if (++bs == kBStages) { bs = 0; bph ^= 1u; }
         }
@@ -456,7 +465,7 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
           ok = wait_or_fail(&sm.y_full[pw % kYSlots], (uint32_t)(((P * 12 + pw) / kYSlots) & 1), fail);
         }
         int const ac = P * kChunks + c, as = ac % kAStages;
-        if (!ok || !wait_or_fail(&sm.a_empty[as], (uint32_t)(((ac / kAStages) & 1) ^ 1), fail)) { ok = false; break; }
+        if (!ok || !wait_or_fail(&sm.empty[as], (uint32_t)(((ac / kAStages) & 1) ^ 1), fail)) { ok = false; break; }
         int const pq0 = 8 * c + 2 * j, p = pq0 / 12, q0 = pq0 % 12;  // pq0, pq0 + 1 share p
         // k = 4j .. 4j+3: core column j, the whole 16-byte row (mu*32 + s)
         float* Ahi = sm.A[as][0] + j * 16 * 32 + s * 4;
