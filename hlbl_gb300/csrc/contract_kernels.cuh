@@ -621,7 +621,8 @@ static __global__ void qed_weights_fp32_kernel(Geometry geo, WArgs args, double 
       double ww[HLBL_QED_NW];
       {
         float wf[HLBL_QED_NW];
-        weights_f32<false, false>(qf, X, cc, Y, wf);
+        if (qf.geometric) weights_f32<true, false>(qf, X, cc, Y, wf);
+        else weights_f32<false, false>(qf, X, cc, Y, wf);
 #pragma unroll
         for (int j = 0; j < HLBL_QED_NW; ++j) ww[j] = (double)wf[j];
       }

@@ -20,6 +20,7 @@ struct QedF32 {
   float e2[HLBL_QED_NW];
   int geometric;            // m_j = m_0 + j dm for every j
   float de2;                // -dm log2(e)
+  float dmneg;              // -dm
   float uu[HLBL_QED_NQ], vv[HLBL_QED_NQ], uv2[HLBL_QED_NQ];
   float wh[HLBL_QED_NQ][HLBL_QED_NW];
   float mneg[HLBL_QED_NW];  // -m_j
@@ -38,6 +39,7 @@ inline void qed_f32_tables(const hlbl_qed_params& qp, QedF32& q) {
   for (int j = 2; j < 6; ++j)
     if (fabs(qp.mass[j] - (qp.mass[0] + j * dm)) > 1e-12 * fabs(qp.mass[j])) q.geometric = 0;
   q.de2 = (float)(-dm * log2e);
+  q.dmneg = (float)(-dm);
   for (int i = 0; i < HLBL_QED_NQ; ++i) {
     double const u = qp.node[i], v = 1.0 - u;
     q.uu[i] = (float)(u * u);
@@ -74,8 +76,10 @@ __device__ __forceinline__ float ex2_approx(float x) {
 // per term), and with masses in arithmetic progression (m_j = m_0 + j dm, the
 // stand-in's) exp(-m_0 r) g_i/(1+R^2) times powers of exp(-dm r): two
 // operations per weight and node. Otherwise the correctly rounded FP32
-// division, square root and expf per weight (the kernel-sum path, whose
-// chain total is held to 1e-6).
+// division and square root and expf (the kernel-sum path, whose chain total
+// is held to 1e-6): with GEOM two expf per node and the powers of
+// exp(-dm r) by five roundings to nearest (unbiased, a few 1e-7 at j = 5),
+// else one expf per weight.
 template <bool GEOM, bool FAST = true>
 __device__ __forceinline__ void weights_f32(const QedF32& q, float X, float c, float Y, float w[6]) {
   float const X2 = X * X, Y2 = Y * Y, XYc = X * Y * c;
@@ -106,8 +110,18 @@ __device__ __forceinline__ void weights_f32(const QedF32& q, float X, float c, f
     } else {
       float const g = 1.f / (1.f + r2);
       float const r = sqrtf(r2 + q.l2);
+      if constexpr (GEOM) {
+        float te = g * expf(q.mneg[0] * r);
+        float const de = expf(q.dmneg * r);
 #pragma unroll
-      for (int j = 0; j < 6; ++j) w[j] = fmaf(q.wh[i][j] * g, expf(q.mneg[j] * r), w[j]);
+        for (int j = 0; j < 6; ++j) {
+          w[j] = fmaf(q.wh[i][j], te, w[j]);
+          if (j < 5) te *= de;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 6; ++j) w[j] = fmaf(q.wh[i][j] * g, expf(q.mneg[j] * r), w[j]);
+      }
     }
   }
 }
