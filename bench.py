@@ -463,6 +463,10 @@ def main():
 
     def e2e_pass():
         h2d = d2h = 0
+        # device timestamps on the compute stream: the pass's start and each
+        # step's end (a step also waits there for its staged block)
+        evs = [torch.cuda.Event(enable_timing=True)]
+        evs[0].record(stream)
         site0 = schedule.mod_pos(timed[0][0], LATTICE)
         # each source's block has its own device buffer, idle while it is staged
         c.stage_async(block(timed[0][0]), pinned[site0], pinned[site0].numel() * 8, after_compute=False)
@@ -481,11 +485,14 @@ def main():
                 h2d += pinned[sn].numel() * 8
             with torch.cuda.stream(stream):
                 host_out[k:k + len(xs)].copy_(res[k:k + len(xs)], non_blocking=True)
+            evs.append(torch.cuda.Event(enable_timing=True))
+            evs[-1].record(stream)
             d2h += len(xs) * 16
             k += len(xs)
         enq = time.perf_counter()
         stream.synchronize()
-        return h2d, d2h, enq
+        steps_ms = [round(a.elapsed_time(b), 1) for a, b in zip(evs[:-1], evs[1:])]
+        return h2d, d2h, enq, steps_ms
 
     # one untimed pass first (the first copies from freshly pinned pages and
     # the first launches of this call sequence are not representative), then
@@ -493,7 +500,7 @@ def main():
     # same work have measured 45 and 139 pairs/s in one run), so the median
     # is reported and all seven are listed, each with the host time spent
     # enqueueing it (a slow pass with a short enqueue time waited on the device)
-    e2e_pass()
+    e2e_pass()  # untimed
     # a 1 GB pinned host -> device copy just before each pass: the host link's
     # bandwidth at that moment (the machine's host side is shared)
     probe_h = torch.empty(1 << 30, dtype=torch.uint8, pin_memory=True)
@@ -508,16 +515,17 @@ def main():
         e1.synchronize()
         return (1 << 30) / (e0.elapsed_time(e1) * 1e-3) / 1e9
 
-    e2e_runs, e2e_enq, h2d_gbs = [], [], []
+    e2e_runs, e2e_enq, e2e_steps, h2d_gbs = [], [], [], []
     for _ in range(7):
         h2d_gbs.append(round(h2d_probe(), 1))
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
-        h2d, d2h, enq = e2e_pass()
+        h2d, d2h, enq, steps_ms = e2e_pass()
         e2e_runs.append(time.perf_counter() - t0)
         e2e_enq.append(enq - t0)
+        e2e_steps.append(steps_ms)
     del probe_h, probe_d
     e2e_s = statistics.median(e2e_runs)
     if dist:
@@ -615,6 +623,7 @@ def main():
                 "d2h_bytes_per_step": int(d2h / max(1, len(timed))),
                 "passes_pairs_per_s": [round(pairs_total / t, 2) for t in e2e_runs],
                 "passes_enqueue_ms": [round(1e3 * t, 1) for t in e2e_enq],
+                "passes_step_ms": e2e_steps,
                 "h2d_probe_gbs_before_each_pass": h2d_gbs,
                 "how": "median of seven passes over the timed steps after one untimed pass; each "
                        "step stages its new block from pinned host memory on the side stream while "
