@@ -16,10 +16,10 @@
 //   1      TMA producer of the B chunks (16 k x 160 n, hi and lo, 20 KB) -- one thread
 //   2      TMEM allocation; tcgen05.mma issue and commits -- one thread
 //   3-10   D formation, two groups of four warps on alternate chunks of
-//          16 k (8 (p, q)): warp j of a group forms the chunk's j-th pair of
-//          (p, q) (one Y row, two S rows) for its lane's site: O = Y conj(S)
-//          spin blocks -> D_mu -> hi/lo -> shared memory in the K-major
-//          no-swizzle core-matrix layout
+//          16 k (8 (p, q): half of a block of 4 p x 4 q): warp j of a group
+//          forms the chunk's j-th pair of (p, q) (one Y row, two S rows) for
+//          its lane's site: O = Y conj(S) spin blocks -> D_mu -> hi/lo ->
+//          shared memory in the K-major no-swizzle core-matrix layout
 //   11-14  epilogue: one TMEM lane quadrant each (warp % 4 = mu); per phase,
 //          the F rows from TMEM dotted with the QED coefficients of the
 //          row's site, into a compensated FP64 sum
@@ -33,7 +33,8 @@
 // dot. The two main buffers swap roles every phase: the next phase's first
 // half only waits for that fold, its second half for the dot.
 // Pipelines (mbarriers; every wait bounded, kWaitLimit polls):
-//   rows -> D warps (S double buffer per phase, Y ring of 3 rows),
+//   rows -> D warps (S rows of a block in a ring of 3 blocks, Y rows of a
+//   p-block in a ring of 2),
 //   D warps -> MMA (A ring of 4), B producer -> MMA (B ring of 4), one
 //   commit per chunk frees both stages,
 //   MMA -> epilogue (acc_full), epilogue -> MMA (folded, dotted).
@@ -62,9 +63,15 @@ constexpr int kChunks = kBtK / kKc;        // 18
 // A and B rings of the same depth, released by one commit per chunk: the
 // tensor pipe's completion reaches the waiting producers about 2,500 cycles
 // after a chunk is issued, so four chunks (about 2,400 cycles of MMAs) must
-// be in flight to keep it busy; three Y rows cover the 16 (p, q) of two
-// chunks in flight per D group
-constexpr int kStages = 4, kAStages = kStages, kBStages = kStages, kYSlots = 3;
+// be in flight to keep it busy.
+constexpr int kStages = 4, kAStages = kStages, kBStages = kStages;
+// K order: blocks of 4 p x 4 q (two chunks each), q-blocks inner, so both row
+// sets stream through small rings instead of one being held for a whole
+// phase: the S rows 4 bq..4 bq+3 of a block (a ring of three blocks) and the
+// Y rows 4 bp..4 bp+3 of a p-block (a ring of two); the S rows are fetched
+// again (from L2) for each p-block.
+constexpr int kRowsPerGroup = 4, kSGroups = 3, kYGroups = 2, kBlocksQ = 3;
+constexpr int kBlocks = 9;  // per phase: 3 p-blocks x 3 q-blocks
 constexpr int kHalf = kChunks / 2;               // chunks per main-accumulator half
 constexpr uint32_t kCorrCol = 2 * kBtN;          // the correction accumulator's first column
 constexpr int kAPart = kM * kKc;           // floats per A part (hi or lo)
@@ -82,11 +89,11 @@ constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kBt
                             ((uint32_t)(kM >> 4) << 24);
 
 struct __align__(1024) Smem {
-  float S[2][12][kRowF32];
-  float Y[kYSlots][kRowF32];
+  float S[kSGroups][kRowsPerGroup][kRowF32];
+  float Y[kYGroups][kRowsPerGroup][kRowF32];
   float A[kAStages][2][kAPart];
   float B[kBStages][2][kBPart];
-  uint64_t s_full[2], s_empty[2], y_full[kYSlots], y_empty[kYSlots];
+  uint64_t s_full[kSGroups], s_empty[kSGroups], y_full[kYGroups], y_empty[kYGroups];
   uint64_t a_full[kStages], b_full[kStages], empty[kStages];
   uint64_t acc_full, folded, dotted, mma_done;
   uint32_t taddr;
@@ -316,8 +323,8 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
   };
 
   if (t == 0) {
-    for (int i = 0; i < 2; ++i) { mbar_init(&sm.s_full[i], 1); mbar_init(&sm.s_empty[i], kDWarps); }
-    for (int i = 0; i < kYSlots; ++i) { mbar_init(&sm.y_full[i], 1); mbar_init(&sm.y_empty[i], kDWarps); }
+    for (int i = 0; i < kSGroups; ++i) { mbar_init(&sm.s_full[i], 1); mbar_init(&sm.s_empty[i], kDWarps); }
+    for (int i = 0; i < kYGroups; ++i) { mbar_init(&sm.y_full[i], 1); mbar_init(&sm.y_empty[i], kDWarps); }
     for (int i = 0; i < kStages; ++i) {
       mbar_init(&sm.a_full[i], kDGroup);
       mbar_init(&sm.b_full[i], 1);
@@ -341,38 +348,38 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
   uint32_t const tmem = sm.taddr;
 
   // issue tracking for the teardown after a failure
-  int rows_issued_s = -1, rows_issued_y = -1;  // last phase / row-use index issued
+  int rows_issued_s = -1, rows_issued_y = -1;  // last S block / Y p-block use issued
   int b_issued = -1;
   bool mma_any = false;
 
   if (warp == kWarpRows) {
     // ---- input rows ---------------------------------------------------------
+    // per phase, in the order the D warps use them: the Y rows of p-block bp,
+    // then the S rows of its three blocks. A wait here is for the ring slot
+    // of a use two (Y) or three (S) steps back, whose readers need only rows
+    // issued before it.
     if (lane == 0 && nph > 0) {
-      auto issue_S = [&](int P) -> bool {
-        int const buf = P & 1, f = P & 1;
-        long long const tile = blockIdx.x + (long long)(P >> 1) * gridDim.x;
-        if (!wait_or_fail(&sm.s_empty[buf], (uint32_t)(((P >> 1) & 1) ^ 1), fail)) return false;
-        fence_proxy_async_smem();
-        mbar_arrive_expect_tx(&sm.s_full[buf], 12 * kRowBytes);
-        for (int q = 0; q < 12; ++q) bulk_g2s(sm.S[buf][q], row_ptr(x32, 1 - f, q, tile), kRowBytes, &sm.s_full[buf]);
-        rows_issued_s = P;
-        return true;
-      };
-      bool ok = issue_S(0);
+      bool ok = true;
       for (int P = 0; ok && P < nph; ++P) {
         int const f = P & 1;
         long long const tile = blockIdx.x + (long long)(P >> 1) * gridDim.x;
-        for (int p = 0; ok && p < 12; ++p) {
-          int const uy = P * 12 + p, slot = p % kYSlots;
-          if (!wait_or_fail(&sm.y_empty[slot], (uint32_t)(((uy / kYSlots) & 1) ^ 1), fail)) { ok = false; break; }
+        for (int bp = 0; ok && bp < 3; ++bp) {
+          int const uy = P * 3 + bp, ys = uy % kYGroups;
+          if (!wait_or_fail(&sm.y_empty[ys], (uint32_t)(((uy / kYGroups) & 1) ^ 1), fail)) { ok = false; break; }
           fence_proxy_async_smem();
-          mbar_arrive_expect_tx(&sm.y_full[slot], kRowBytes);
-          bulk_g2s(sm.Y[slot], row_ptr(y32, f, p, tile), kRowBytes, &sm.y_full[slot]);
+          mbar_arrive_expect_tx(&sm.y_full[ys], kRowsPerGroup * kRowBytes);
+          for (int r = 0; r < kRowsPerGroup; ++r)
+            bulk_g2s(sm.Y[ys][r], row_ptr(y32, f, 4 * bp + r, tile), kRowBytes, &sm.y_full[ys]);
           rows_issued_y = uy;
-          // the next phase's S rows into the other buffer, once its readers
-          // (the previous phase) are done: issuing row kYSlots needed row 0
-          // of this phase consumed, so that wait no longer blocks the Y rows
-          if (p == kYSlots && P + 1 < nph) ok = issue_S(P + 1);
+          for (int bq = 0; ok && bq < kBlocksQ; ++bq) {
+            int const us = P * kBlocks + bp * kBlocksQ + bq, ss = us % kSGroups;
+            if (!wait_or_fail(&sm.s_empty[ss], (uint32_t)(((us / kSGroups) & 1) ^ 1), fail)) { ok = false; break; }
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&sm.s_full[ss], kRowsPerGroup * kRowBytes);
+            for (int r = 0; r < kRowsPerGroup; ++r)
+              bulk_g2s(sm.S[ss][r], row_ptr(x32, 1 - f, 4 * bq + r, tile), kRowBytes, &sm.s_full[ss]);
+            rows_issued_s = us;
+          }
         }
       }
     }
@@ -455,23 +462,23 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
     for (int P = 0; ok && P < nph; ++P) {
       long long const tile = blockIdx.x + (long long)(P >> 1) * gridDim.x;
       int const nvalid = (int)min((long long)kSites, geo.V - tile * kSites);
-      if (!wait_or_fail(&sm.s_full[P & 1], (uint32_t)((P >> 1) & 1), fail)) break;
-      const float* Sb = sm.S[P & 1][0];
-      int pw = -1;  // Y rows of this phase waited for
       for (int c = grp; c < kChunks; c += kDWarps / kDGroup) {
-        int const pmax = (8 * c + 7) / 12;
-        while (ok && pw < pmax) {
-          ++pw;
-          ok = wait_or_fail(&sm.y_full[pw % kYSlots], (uint32_t)(((P * 12 + pw) / kYSlots) & 1), fail);
-        }
+        // chunk c is half c & 1 (= grp) of block b = (bp, bq): this warp's
+        // pair is p = 4 bp + 2 grp + j/2 (row p_in of the Y group) and
+        // q = 4 bq + q_in, q_in + 1 (rows of the S group), q_in = 2 (j & 1)
+        int const b = c >> 1, bp = b / kBlocksQ, bq = b - bp * kBlocksQ;
+        int const uy = P * 3 + bp, ys = uy % kYGroups;
+        int const us = P * kBlocks + b, ss = us % kSGroups;
+        if (bq == 0) ok = ok && wait_or_fail(&sm.y_full[ys], (uint32_t)((uy / kYGroups) & 1), fail);
+        ok = ok && wait_or_fail(&sm.s_full[ss], (uint32_t)((us / kSGroups) & 1), fail);
         int const ac = P * kChunks + c, as = ac % kAStages;
         if (!ok || !wait_or_fail(&sm.empty[as], (uint32_t)(((ac / kAStages) & 1) ^ 1), fail)) { ok = false; break; }
-        int const pq0 = 8 * c + 2 * j, p = pq0 / 12, q0 = pq0 % 12;  // pq0, pq0 + 1 share p
+        int const p_in = 2 * grp + (j >> 1), q_in = 2 * (j & 1);
         // k = 4j .. 4j+3: core column j, the whole 16-byte row (mu*32 + s)
         float* Ahi = sm.A[as][0] + j * 16 * 32 + s * 4;
         float* Alo = sm.A[as][1] + j * 16 * 32 + s * 4;
         if (s < nvalid) {
-          const float* Yr = sm.Y[p % kYSlots] + f32_tile_off(s, 0);
+          const float* Yr = sm.Y[ys][p_in] + f32_tile_off(s, 0);
           float y[24];
 #pragma unroll
           for (int c4 = 0; c4 < 6; ++c4) {
@@ -481,7 +488,7 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
           float d[4][4];  // [mu][pq0 re, pq0 im, pq1 re, pq1 im]
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
-            const float* Sr = Sb + (q0 + h) * kRowF32 + f32_tile_off(s, 0);
+            const float* Sr = sm.S[ss][q_in + h] + f32_tile_off(s, 0);
             float x[24];
 #pragma unroll
             for (int c4 = 0; c4 < 6; ++c4) {
@@ -537,18 +544,12 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
         __syncwarp();
         if (lane == 0) {
           mbar_arrive(&sm.a_full[as]);
-          // Y rows whose last chunk in this group this was (each group
-          // arrives once per row: every row spans chunks of both groups)
-          for (int pp = (8 * c) / 12; pp <= pmax; ++pp) {
-            int const last = (12 * pp + 11) / 8;
-            int const last_g = last - ((last - grp) & 1);  // the group's last chunk using pp
-            if (last_g == c) mbar_arrive(&sm.y_empty[pp % kYSlots]);
-          }
+          // every D warp reads each S block in one chunk and each Y group
+          // in three (bq = 0..2)
+          mbar_arrive(&sm.s_empty[ss]);
+          if (bq == kBlocksQ - 1) mbar_arrive(&sm.y_empty[ys]);
         }
       }
-      if (!ok) break;
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&sm.s_empty[P & 1]);
     }
   } else {
     // ---- epilogue -----------------------------------------------------------------------
@@ -642,9 +643,10 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
   if (*fail) {
     // let nothing this CTA started outlive it (each wait bounded)
     if (warp == kWarpRows && lane == 0) {
-      if (rows_issued_s >= 0) mbar_wait(&sm.s_full[rows_issued_s & 1], (uint32_t)((rows_issued_s >> 1) & 1));
-      for (int u = rows_issued_y - kYSlots + 1; u <= rows_issued_y; ++u)
-        if (u >= 0) mbar_wait(&sm.y_full[u % kYSlots], (uint32_t)((u / kYSlots) & 1));
+      for (int u = rows_issued_s - kSGroups + 1; u <= rows_issued_s; ++u)
+        if (u >= 0) mbar_wait(&sm.s_full[u % kSGroups], (uint32_t)((u / kSGroups) & 1));
+      for (int u = rows_issued_y - kYGroups + 1; u <= rows_issued_y; ++u)
+        if (u >= 0) mbar_wait(&sm.y_full[u % kYGroups], (uint32_t)((u / kYGroups) & 1));
     }
     if (warp == kWarpB && lane == 0)
       for (int u = b_issued - kBStages + 1; u <= b_issued; ++u)
@@ -679,7 +681,11 @@ __global__ void btu_build_kernel(const double* __restrict__ g, int nf, float* __
   const double* g_dzu = g + ((size_t)pi * nf + fl) * kGLen;
   const double* g_dzsu = g_dzu + kGDzuLen;
   int const k = i / kBtN, n = i % kBtN;
-  int const e = k & 1, pq = k >> 1, p = pq / 12, q = pq % 12;
+  // k within chunk c: 4 jj + 2 hh + e for the pair (p, q) the D formation
+  // puts there (block b = c/2 of 4 p x 4 q, half c & 1)
+  int const cc = k / kKc, kl = k % kKc, jj = kl >> 2, hh = (kl >> 1) & 1, e = kl & 1;
+  int const bb = cc >> 1, bbp = bb / kBlocksQ, bbq = bb - bbp * kBlocksQ;
+  int const p = 4 * bbp + 2 * (cc & 1) + (jj >> 1), q = 4 * bbq + 2 * (jj & 1) + hh;
   int const lam = n & 3, nu = (n >> 2) & 3, j = n >> 4;
   int const sq = q / 3, cq = q % 3;
   int sq2 = 0;
