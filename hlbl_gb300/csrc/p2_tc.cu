@@ -64,7 +64,10 @@ constexpr int kChunks = kBtK / kKc;        // 18
 // tensor pipe's completion reaches the waiting producers about 2,500 cycles
 // after a chunk is issued, so four chunks (about 2,400 cycles of MMAs) must
 // be in flight to keep it busy.
-constexpr int kStages = 4, kAStages = kStages, kBStages = kStages;
+constexpr int kAStages = 4, kBStages = 4;
+// equal depths: one commit per chunk frees the A and the B stage (a fifth A
+// or B stage with a second commit per chunk measured 2-4 % slower)
+constexpr bool kSharedEmpty = kAStages == kBStages;
 // K order: blocks of 4 p x 4 q (two chunks each), q-blocks inner, so both row
 // sets stream through small rings instead of one being held for a whole
 // phase: the S rows 4 bq..4 bq+3 of a block (a ring of three blocks) and the
@@ -94,7 +97,7 @@ struct __align__(1024) Smem {
   float A[kAStages][2][kAPart];
   float B[kBStages][2][kBPart];
   uint64_t s_full[kSGroups], s_empty[kSGroups], y_full[kYGroups], y_empty[kYGroups];
-  uint64_t a_full[kStages], b_full[kStages], empty[kStages];
+  uint64_t a_full[kAStages], b_full[kBStages], a_empty[kAStages], b_empty[kBStages];
   uint64_t acc_full, folded, dotted, mma_done;
   uint32_t taddr;
   int fail;
@@ -325,11 +328,8 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
   if (t == 0) {
     for (int i = 0; i < kSGroups; ++i) { mbar_init(&sm.s_full[i], 1); mbar_init(&sm.s_empty[i], kDWarps); }
     for (int i = 0; i < kYGroups; ++i) { mbar_init(&sm.y_full[i], 1); mbar_init(&sm.y_empty[i], kDWarps); }
-    for (int i = 0; i < kStages; ++i) {
-      mbar_init(&sm.a_full[i], kDGroup);
-      mbar_init(&sm.b_full[i], 1);
-      mbar_init(&sm.empty[i], 1);
-    }
+    for (int i = 0; i < kAStages; ++i) { mbar_init(&sm.a_full[i], kDGroup); mbar_init(&sm.a_empty[i], 1); }
+    for (int i = 0; i < kBStages; ++i) { mbar_init(&sm.b_full[i], 1); mbar_init(&sm.b_empty[i], 1); }
     mbar_init(&sm.acc_full, 1);
     mbar_init(&sm.folded, kEWarps);
     mbar_init(&sm.dotted, kEWarps);
@@ -392,7 +392,8 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
         const float* src = btu + ((size_t)pi * 2 + (P & 1)) * kChunks * 2 * kBPart;
         for (int c = 0; c < kChunks; ++c, ++bc) {
           int const st = bc % kBStages;
-          if (!wait_or_fail(&sm.empty[st], (uint32_t)(((bc / kBStages) & 1) ^ 1), fail)) { ok = false; break; }
+          uint64_t* const freed = kSharedEmpty ? &sm.a_empty[st] : &sm.b_empty[st];
+          if (!wait_or_fail(freed, (uint32_t)(((bc / kBStages) & 1) ^ 1), fail)) { ok = false; break; }
           fence_proxy_async_smem();
           mbar_arrive_expect_tx(&sm.b_full[st], 2 * kBPart * 4);
           bulk_g2s(sm.B[st][0], src + (size_t)c * 2 * kBPart, 2 * kBPart * 4, &sm.b_full[st]);
@@ -445,7 +446,8 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
           mma_tf32(dc, ahi + kAK16, bhi + kBK16 + kBLo16, 1u);
           mma_tf32(dc, ahi + kAK16 + kALo16, bhi + kBK16, 1u);
           mma_any = true;
-          mma_commit(&sm.empty[as]);  // frees A and B stage as (= bs)
+          mma_commit(&sm.a_empty[as]);  // with equal depths also B stage bs (= as)
+          if constexpr (!kSharedEmpty) mma_commit(&sm.b_empty[bs]);
           if (++as == kAStages) { as = 0; aph ^= 1u; }
           if (++bs == kBStages) { bs = 0; bph ^= 1u; }
         }
@@ -472,7 +474,7 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
         if (bq == 0) ok = ok && wait_or_fail(&sm.y_full[ys], (uint32_t)((uy / kYGroups) & 1), fail);
         ok = ok && wait_or_fail(&sm.s_full[ss], (uint32_t)((us / kSGroups) & 1), fail);
         int const ac = P * kChunks + c, as = ac % kAStages;
-        if (!ok || !wait_or_fail(&sm.empty[as], (uint32_t)(((ac / kAStages) & 1) ^ 1), fail)) { ok = false; break; }
+        if (!ok || !wait_or_fail(&sm.a_empty[as], (uint32_t)(((ac / kAStages) & 1) ^ 1), fail)) { ok = false; break; }
         int const p_in = 2 * grp + (j >> 1), q_in = 2 * (j & 1);
         // k = 4j .. 4j+3: core column j, the whole 16-byte row (mu*32 + s)
         float* Ahi = sm.A[as][0] + j * 16 * 32 + s * 4;
