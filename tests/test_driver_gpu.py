@@ -84,14 +84,16 @@ def test_driver_device_host_batched_graphs():
             assert c.kernel_sum(d_x, d_y, r.x, r.yv, xu, hg.FP64) == r.kernel_sum
 
 
-def test_run_chains_equals_independent_chains():
+def test_run_chains_equals_independent_chains(tmp_path):
     """Two chains over one cache (driver.cpp:169-208) give the pairs and sums
-    of each chain run alone (test_driver_random.cpp's two-chain check), and
-    the 2+2 of a source solved by both chains is computed once."""
+    of each chain run alone (test_driver_random.cpp's two-chain check), the
+    2+2 of a source solved by both chains is computed once, and the result
+    file holds the in-memory results bit for bit (test_driver_random.cpp:351-352)."""
     import hlbl_gb300 as hg
     from hlbl_gb300 import schedule
     from hlbl_gb300.cache import PropagatorCache, TorchBuffers
     from hlbl_gb300.driver import run_chain, run_chains
+    from hlbl_gb300.output import Chain, ResultWriter, RunInfo, TimingLog, read_results
 
     lat = (6, 6, 6, 6)
     xu = hg.xunit(105.6583745, 0.07957)
@@ -102,8 +104,15 @@ def test_run_chains_equals_independent_chains():
 
         out22 = []
         cache = PropagatorCache("device", c.block_length, TorchBuffers(c))
+        info = RunInfo(lattice=lat, chains=[Chain((0, 0, 0, 0), (1, 1, 1, 1), 1, 1),
+                                            Chain((0, 0, 0, 0), (-1, 1, -1, 1), 1, 1)],
+                       xunit=xu, with_2p2=True)
+        writer = ResultWriter(str(tmp_path / "run.npz"), info)
+        timing = TimingLog(str(tmp_path / "timing.csv"))
         res, st, _ = run_chains(chains, lat, xu, provider, c, cache, precision=hg.FP32,
-                                sources_2p2=[((0, 0, 0, 0), [(1, 1, 1, 1)])], results_2p2=out22)
+                                sources_2p2=[((0, 0, 0, 0), [(1, 1, 1, 1)])], results_2p2=out22,
+                                writer=writer, timing=timing)
+        timing.close()
         alone = []
         for i, ch in enumerate(chains):
             r, _ = run_chain(ch, lat, xu, provider, c, PropagatorCache("device", c.block_length,
@@ -113,3 +122,12 @@ def test_run_chains_equals_independent_chains():
         assert [(r.x, r.y, r.yv, r.chain) for r in res] == [(r.x, r.y, r.yv, r.chain) for r in alone]
         assert [r.kernel_sum for r in res] == [r.kernel_sum for r in alone]
         assert len(out22) == 1 and out22[0].chain == 0 and st.pieces_2p2 == 1
+        f = read_results(str(tmp_path / "run.npz"))
+        assert np.array_equal(f["kernel_sum/kernel_sum"], np.array([r.kernel_sum for r in res]))
+        assert [tuple(v) for v in f["kernel_sum/x"]] == [r.x for r in res]
+        assert [tuple(v) for v in f["kernel_sum/yv"]] == [tuple(r.yv) for r in res]
+        assert list(f["kernel_sum/chain"]) == [r.chain for r in res]
+        assert np.array_equal(f["2p2/P1"][0], np.asarray(out22[0].p1).reshape(4, 4, 4, max(lat)))
+        assert np.array_equal(f["2p2/P234"].reshape(-1, 5, 64), np.asarray(out22[0].p234).reshape(-1, 5, 64))
+        rows = open(tmp_path / "timing.csv").read().splitlines()[1:]
+        assert sum(r.startswith("kernel_sum,") for r in rows) == st.pairs
