@@ -33,9 +33,9 @@
 // dot. The two main buffers swap roles every phase: the next phase's first
 // half only waits for that fold, its second half for the dot.
 // Pipelines (mbarriers; every wait bounded, kWaitLimit polls):
-//   rows -> D warps (S rows of a block in a ring of 3 blocks, Y rows of a
-//   p-block in a ring of 2),
-//   D warps -> MMA (A ring of 4), B producer -> MMA (B ring of 4), one
+//   rows -> D warps (S rows of a block in a ring of 2 blocks, Y rows of a
+//   p-block by halves in a ring of 3),
+//   D warps -> MMA (A ring of 5), B producer -> MMA (B ring of 5), one
 //   commit per chunk frees both stages,
 //   MMA -> epilogue (acc_full), epilogue -> MMA (folded, dotted).
 //
@@ -64,16 +64,18 @@ constexpr int kChunks = kBtK / kKc;        // 18
 // tensor pipe's completion reaches the waiting producers about 2,500 cycles
 // after a chunk is issued, so four chunks (about 2,400 cycles of MMAs) must
 // be in flight to keep it busy.
-constexpr int kAStages = 4, kBStages = 4;
-// equal depths: one commit per chunk frees the A and the B stage (a fifth A
-// or B stage with a second commit per chunk measured 2-4 % slower)
+constexpr int kAStages = 5, kBStages = 5;
+// equal depths: one commit per chunk frees the A and the B stage (a deeper
+// ring for one of them with a second commit per chunk measured slower)
 constexpr bool kSharedEmpty = kAStages == kBStages;
 // K order: blocks of 4 p x 4 q (two chunks each), q-blocks inner, so both row
 // sets stream through small rings instead of one being held for a whole
-// phase: the S rows 4 bq..4 bq+3 of a block (a ring of three blocks) and the
-// Y rows 4 bp..4 bp+3 of a p-block (a ring of two); the S rows are fetched
-// again (from L2) for each p-block.
-constexpr int kRowsPerGroup = 4, kSGroups = 3, kYGroups = 2, kBlocksQ = 3;
+// phase: the S rows 4 bq..4 bq+3 of a block (a ring of two blocks; fetched
+// again, from L2, for each p-block) and the Y rows of a p-block by halves,
+// half h (rows 4 bp + 2h, 4 bp + 2h + 1) read only by D group h (a ring of
+// three halves). This leaves room for five A and B stages.
+constexpr int kRowsPerGroup = 4, kSGroups = 2, kBlocksQ = 3;
+constexpr int kYRows = 2, kYSlots = 3;
 constexpr int kBlocks = 9;  // per phase: 3 p-blocks x 3 q-blocks
 constexpr int kHalf = kChunks / 2;               // chunks per main-accumulator half
 constexpr uint32_t kCorrCol = 2 * kBtN;          // the correction accumulator's first column
@@ -93,10 +95,10 @@ constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kBt
 
 struct __align__(1024) Smem {
   float S[kSGroups][kRowsPerGroup][kRowF32];
-  float Y[kYGroups][kRowsPerGroup][kRowF32];
+  float Y[kYSlots][kYRows][kRowF32];
   float A[kAStages][2][kAPart];
   float B[kBStages][2][kBPart];
-  uint64_t s_full[kSGroups], s_empty[kSGroups], y_full[kYGroups], y_empty[kYGroups];
+  uint64_t s_full[kSGroups], s_empty[kSGroups], y_full[kYSlots], y_empty[kYSlots];
   uint64_t a_full[kAStages], b_full[kBStages], a_empty[kAStages], b_empty[kBStages];
   uint64_t acc_full, folded, dotted, mma_done;
   uint32_t taddr;
@@ -327,7 +329,7 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
 
   if (t == 0) {
     for (int i = 0; i < kSGroups; ++i) { mbar_init(&sm.s_full[i], 1); mbar_init(&sm.s_empty[i], kDWarps); }
-    for (int i = 0; i < kYGroups; ++i) { mbar_init(&sm.y_full[i], 1); mbar_init(&sm.y_empty[i], kDWarps); }
+    for (int i = 0; i < kYSlots; ++i) { mbar_init(&sm.y_full[i], 1); mbar_init(&sm.y_empty[i], kDGroup); }
     for (int i = 0; i < kAStages; ++i) { mbar_init(&sm.a_full[i], kDGroup); mbar_init(&sm.a_empty[i], 1); }
     for (int i = 0; i < kBStages; ++i) { mbar_init(&sm.b_full[i], 1); mbar_init(&sm.b_empty[i], 1); }
     mbar_init(&sm.acc_full, 1);
@@ -364,13 +366,15 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
         int const f = P & 1;
         long long const tile = blockIdx.x + (long long)(P >> 1) * gridDim.x;
         for (int bp = 0; ok && bp < 3; ++bp) {
-          int const uy = P * 3 + bp, ys = uy % kYGroups;
-          if (!wait_or_fail(&sm.y_empty[ys], (uint32_t)(((uy / kYGroups) & 1) ^ 1), fail)) { ok = false; break; }
-          fence_proxy_async_smem();
-          mbar_arrive_expect_tx(&sm.y_full[ys], kRowsPerGroup * kRowBytes);
-          for (int r = 0; r < kRowsPerGroup; ++r)
-            bulk_g2s(sm.Y[ys][r], row_ptr(y32, f, 4 * bp + r, tile), kRowBytes, &sm.y_full[ys]);
-          rows_issued_y = uy;
+          for (int h = 0; ok && h < 2; ++h) {
+            int const uy = (P * 3 + bp) * 2 + h, ys = uy % kYSlots;
+            if (!wait_or_fail(&sm.y_empty[ys], (uint32_t)(((uy / kYSlots) & 1) ^ 1), fail)) { ok = false; break; }
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&sm.y_full[ys], kYRows * kRowBytes);
+            for (int r = 0; r < kYRows; ++r)
+              bulk_g2s(sm.Y[ys][r], row_ptr(y32, f, 4 * bp + 2 * h + r, tile), kRowBytes, &sm.y_full[ys]);
+            rows_issued_y = uy;
+          }
           for (int bq = 0; ok && bq < kBlocksQ; ++bq) {
             int const us = P * kBlocks + bp * kBlocksQ + bq, ss = us % kSGroups;
             if (!wait_or_fail(&sm.s_empty[ss], (uint32_t)(((us / kSGroups) & 1) ^ 1), fail)) { ok = false; break; }
@@ -469,13 +473,13 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
         // pair is p = 4 bp + 2 grp + j/2 (row p_in of the Y group) and
         // q = 4 bq + q_in, q_in + 1 (rows of the S group), q_in = 2 (j & 1)
         int const b = c >> 1, bp = b / kBlocksQ, bq = b - bp * kBlocksQ;
-        int const uy = P * 3 + bp, ys = uy % kYGroups;
+        int const uy = (P * 3 + bp) * 2 + grp, ys = uy % kYSlots;  // this group's half
         int const us = P * kBlocks + b, ss = us % kSGroups;
-        if (bq == 0) ok = ok && wait_or_fail(&sm.y_full[ys], (uint32_t)((uy / kYGroups) & 1), fail);
+        if (bq == 0) ok = ok && wait_or_fail(&sm.y_full[ys], (uint32_t)((uy / kYSlots) & 1), fail);
         ok = ok && wait_or_fail(&sm.s_full[ss], (uint32_t)((us / kSGroups) & 1), fail);
         int const ac = P * kChunks + c, as = ac % kAStages;
         if (!ok || !wait_or_fail(&sm.a_empty[as], (uint32_t)(((ac / kAStages) & 1) ^ 1), fail)) { ok = false; break; }
-        int const p_in = 2 * grp + (j >> 1), q_in = 2 * (j & 1);
+        int const p_in = j >> 1, q_in = 2 * (j & 1);  // rows of the Y half and of the S group
         // k = 4j .. 4j+3: core column j, the whole 16-byte row (mu*32 + s)
         float* Ahi = sm.A[as][0] + j * 16 * 32 + s * 4;
         float* Alo = sm.A[as][1] + j * 16 * 32 + s * 4;
@@ -546,8 +550,8 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
         __syncwarp();
         if (lane == 0) {
           mbar_arrive(&sm.a_full[as]);
-          // every D warp reads each S block in one chunk and each Y group
-          // in three (bq = 0..2)
+          // every D warp reads each S block in one chunk; a group reads its
+          // Y half in three (bq = 0..2)
           mbar_arrive(&sm.s_empty[ss]);
           if (bq == kBlocksQ - 1) mbar_arrive(&sm.y_empty[ys]);
         }
@@ -647,8 +651,8 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
     if (warp == kWarpRows && lane == 0) {
       for (int u = rows_issued_s - kSGroups + 1; u <= rows_issued_s; ++u)
         if (u >= 0) mbar_wait(&sm.s_full[u % kSGroups], (uint32_t)((u / kSGroups) & 1));
-      for (int u = rows_issued_y - kYGroups + 1; u <= rows_issued_y; ++u)
-        if (u >= 0) mbar_wait(&sm.y_full[u % kYGroups], (uint32_t)((u / kYGroups) & 1));
+      for (int u = rows_issued_y - kYSlots + 1; u <= rows_issued_y; ++u)
+        if (u >= 0) mbar_wait(&sm.y_full[u % kYSlots], (uint32_t)((u / kYSlots) & 1));
     }
     if (warp == kWarpB && lane == 0)
       for (int u = b_issued - kBStages + 1; u <= b_issued; ++u)
