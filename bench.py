@@ -79,6 +79,12 @@ def volume(lat):
     return lat[0] * lat[1] * lat[2] * lat[3]
 
 
+def workload() -> str:
+    """The workload both arms report (config.workload)."""
+    return (f"lattice {'x'.join(map(str, LATTICE))} (V={volume(LATTICE)}), stride 2, h=(+1,-1,+1,-1), K=4; "
+            "step = the pairs one new source closes (window 1 sources)")
+
+
 def window_steps():
     """(new source, [partners]) of windows >= 1, in solve order."""
     from hlbl_gb300 import schedule
@@ -580,9 +586,7 @@ def main():
         "vs_baseline": None,
         "dtype": "fp32 products, fp64 sums",
         "data": "synthetic: seeded i.i.d. complex Gaussian FP64 propagator blocks, generated on the device",
-        "config": {"workload": f"lattice {'x'.join(map(str, LATTICE))} (V={volume(LATTICE)}), stride 2, "
-                               "h=(+1,-1,+1,-1), K=4; step = the pairs one new source closes "
-                               "(window 1 sources)",
+        "config": {"workload": workload(),
                    "lattice": list(LATTICE), "pairs_timed": n32,
                    "path": "batched per source (autotuned), one CUDA graph for the timed sources; "
                            "blocks as FP32 tile copies (each new block converted once, in its step); "
@@ -828,8 +832,7 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3 * ns / 48, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded i.i.d. complex Gaussian FP64 propagator blocks",
-        "config": {"workload": "24^3x48 (T=48,L=24, V=663552), stride 2, h=(+1,-1,+1,-1), K=4",
-                   "lattice": list(LATTICE)},
+        "config": {"workload": workload(), "lattice": list(LATTICE)},
         "impl": "reference",
         "cpu_baseline": {"value": round(v, 6), "unit": "pairs/s", "cores": cores, "kind": "port",
                          "sample": sample},
