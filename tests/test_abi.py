@@ -86,3 +86,45 @@ def test_device_calls_fail_loudly_without_a_gpu(lib):
 
     with pytest.raises(HlblError):
         check(lib.hlbl_ctx_create(C.byref(h), i4(4, 4, 4, 4), i4(4, 4, 4, 4), i4(0, 0, 0, 0), 0.4, 0))
+
+
+C_PROGRAM = r"""
+#include "hlbl_gb300.h"
+#include <stdio.h>
+#include <string.h>
+int main(void) {
+  const char* v = hlbl_version();
+  hlbl_ctx* ctx = 0;
+  int g[4] = {4, 4, 4, 4}, pc[4] = {0, 0, 0, 0};
+  int rc = hlbl_ctx_create(&ctx, g, g, pc, 0.4, 0);
+  int ok = strstr(v, "sm_103a") != 0 && (rc == 0) == (ctx != 0);
+  if (rc != 0) ok = ok && strlen(hlbl_last_error()) > 0;
+  if (ctx) hlbl_ctx_destroy(ctx);
+  printf("%s %d\n", v, rc);
+  return ok ? 0 : 1;
+}
+"""
+
+
+@pytest.mark.parametrize("lang", ["c", "c++"])
+def test_header_compiles_links_and_runs_from_c_and_cxx(lang, lib, tmp_path):
+    """include/hlbl_gb300.h is a plain C header (usable from the reference's
+    C++ and from C shims): a program compiled with -Wall -Wextra links against
+    the library and runs (without a GPU, context creation fails with a status
+    and a message)."""
+    from hlbl_gb300.build import LIB
+
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip(f"no {lang} compiler")
+    src = tmp_path / ("t.c" if lang == "c" else "t.cpp")
+    src.write_text(C_PROGRAM)
+    exe = tmp_path / "t"
+    libdir = os.path.dirname(LIB)
+    std = "-std=c11" if lang == "c" else "-std=c++17"
+    r = subprocess.run([cc, std, "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"), str(src),
+                        "-L", libdir, "-lhlbl_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, run.stdout + run.stderr
