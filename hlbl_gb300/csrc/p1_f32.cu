@@ -86,19 +86,25 @@ __device__ __forceinline__ void tile_sums(const float* __restrict__ Arow, const 
       A[4 * c4] = a.x; A[4 * c4 + 1] = a.y; A[4 * c4 + 2] = a.z; A[4 * c4 + 3] = a.w;
       B[4 * c4] = b.x; B[4 * c4 + 1] = b.y; B[4 * c4 + 2] = b.z; B[4 * c4 + 3] = b.w;
     }
-    // P[s1][s2] = sum_c conj(B[s1][c]) A[s2][c] for s2 = s1^2 and 3-s1
+    // P[s1][s2] = sum_c conj(B[s1][c]) A[s2][c] for s2 = s1^2 and 3-s1, as
+    // packed FP32 pairs: with y = (Re B, Im B), U = sum_c y Re A and
+    // V = sum_c y Im A (the A part broadcast to both halves), Re P = U.x + V.y
+    // and Im P = V.x - U.y -- two packed FMAs per (c, s2) instead of four
     float pa[4][2], pb[4][2];
 #pragma unroll
     for (int s1 = 0; s1 < 4; ++s1) {
-      float ar = 0, ai = 0, br = 0, bi = 0;
+      float2 ua = make_float2(0.f, 0.f), va = ua, ub = ua, vb = ua;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        float const yr = B[2 * (3 * s1 + c)], yi = B[2 * (3 * s1 + c) + 1];
+        float2 const y = make_float2(B[2 * (3 * s1 + c)], B[2 * (3 * s1 + c) + 1]);
         int const sa = 2 * (3 * (s1 ^ 2) + c), sb = 2 * (3 * (3 - s1) + c);
-        ar += yr * A[sa] + yi * A[sa + 1];  ai += yr * A[sa + 1] - yi * A[sa];
-        br += yr * A[sb] + yi * A[sb + 1];  bi += yr * A[sb + 1] - yi * A[sb];
+        ua = __ffma2_rn(y, make_float2(A[sa], A[sa]), ua);
+        va = __ffma2_rn(y, make_float2(A[sa + 1], A[sa + 1]), va);
+        ub = __ffma2_rn(y, make_float2(A[sb], A[sb]), ub);
+        vb = __ffma2_rn(y, make_float2(A[sb + 1], A[sb + 1]), vb);
       }
-      pa[s1][0] = ar; pa[s1][1] = ai; pb[s1][0] = br; pb[s1][1] = bi;
+      pa[s1][0] = ua.x + va.y; pa[s1][1] = va.x - ua.y;
+      pb[s1][0] = ub.x + vb.y; pb[s1][1] = vb.x - ub.y;
     }
     float const z3 = zhs[s][3];
 #pragma unroll
