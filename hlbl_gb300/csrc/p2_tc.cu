@@ -501,19 +501,25 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
               float4 const b = *reinterpret_cast<const float4*>(Sr + c4 * 64);
               x[4 * c4] = b.x; x[4 * c4 + 1] = b.y; x[4 * c4 + 2] = b.z; x[4 * c4 + 3] = b.w;
             }
-            // O[s1][s2] = sum_c Y[s1][c] conj(S[s2][c]), s2 = s1^2 (a) and 3-s1 (b)
+            // O[s1][s2] = sum_c Y[s1][c] conj(S[s2][c]), s2 = s1^2 (a) and 3-s1 (b),
+            // as packed FP32 pairs: with w = (Re Y, Im Y), U = sum_c w Re S and
+            // V = sum_c w Im S (the S part broadcast), Re O = U.x + V.y and
+            // Im O = U.y - V.x -- two packed FMAs per (c, s2) instead of four
             float oa[4][2], ob[4][2];
 #pragma unroll
             for (int s1 = 0; s1 < 4; ++s1) {
-              float ar = 0, ai = 0, br = 0, bi = 0;
+              float2 ua = make_float2(0.f, 0.f), va = ua, ub = ua, vb = ua;
 #pragma unroll
               for (int cc = 0; cc < 3; ++cc) {
-                float const yr = y[2 * (3 * s1 + cc)], yi = y[2 * (3 * s1 + cc) + 1];
+                float2 const w = make_float2(y[2 * (3 * s1 + cc)], y[2 * (3 * s1 + cc) + 1]);
                 int const sa = 2 * (3 * (s1 ^ 2) + cc), sb = 2 * (3 * (3 - s1) + cc);
-                ar += yr * x[sa] + yi * x[sa + 1];  ai += yi * x[sa] - yr * x[sa + 1];
-                br += yr * x[sb] + yi * x[sb + 1];  bi += yi * x[sb] - yr * x[sb + 1];
+                ua = __ffma2_rn(w, make_float2(x[sa], x[sa]), ua);
+                va = __ffma2_rn(w, make_float2(x[sa + 1], x[sa + 1]), va);
+                ub = __ffma2_rn(w, make_float2(x[sb], x[sb]), ub);
+                vb = __ffma2_rn(w, make_float2(x[sb + 1], x[sb + 1]), vb);
               }
-              oa[s1][0] = ar; oa[s1][1] = ai; ob[s1][0] = br; ob[s1][1] = bi;
+              oa[s1][0] = ua.x + va.y; oa[s1][1] = ua.y - va.x;
+              ob[s1][0] = ub.x + vb.y; ob[s1][1] = ub.y - vb.x;
             }
 #pragma unroll
             for (int mu = 0; mu < 4; ++mu) {
