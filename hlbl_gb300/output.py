@@ -7,7 +7,9 @@ attributes in a NumPy .npz container: dataset "group/name" is the array under
 that key, the attributes of the file and of a group are a JSON object under
 "attrs:/" and "attrs:<group>". As in the reference every append is flushed
 (the file is rewritten in full and renamed into place), so a killed job keeps
-its finished windows.
+its finished windows; `flush_every` = n > 1 rewrites after every n-th append
+instead (the container has no in-place append, so a rewrite costs the whole
+file), and `close()` writes what is pending.
 
   kernel_sum/  one row per pair
     x[N][4], y[N][4], yv[N][4], chain[N], window[N]   int32
@@ -56,11 +58,15 @@ class RunInfo:
 class ResultWriter:
     """output.cpp:131-297 in a .npz container (module docstring)."""
 
-    def __init__(self, path: str, info: RunInfo):
+    def __init__(self, path: str, info: RunInfo, flush_every: int = 1):
         if not info.chains:
             raise RuntimeError("ResultWriter: no chains")
+        if flush_every < 1:
+            raise ValueError("ResultWriter: flush_every must be >= 1")
         self.path = path
         self.info = info
+        self.flush_every = flush_every
+        self._pending = 0
         self.lmax = max(int(a) for a in info.lattice)
         self._ks = {"x": [], "y": [], "yv": [], "chain": [], "window": [], "kernel_sum": []}
         self._p22 = {"w": [], "chain": [], "window": [], "P1": [], "pair_w": [], "pair_y": [],
@@ -111,7 +117,7 @@ class ResultWriter:
             self._ks["chain"].append(r.chain)
             self._ks["window"].append(r.window)
             self._ks["kernel_sum"].append(r.kernel_sum)
-        self._flush()
+        self._appended()
 
     def append_2p2(self, rows) -> None:
         """Result2p2 rows (driver.Result2p2); needs RunInfo.with_2p2."""
@@ -128,7 +134,7 @@ class ResultWriter:
                 self._p22["pair_y"].append(y)
                 self._p22["pair_yv"].append(yv)
                 self._p22["P234"].append(p234[t])
-        self._flush()
+        self._appended()
 
     def _arrays(self):
         def ints(v, shape):
@@ -156,7 +162,18 @@ class ResultWriter:
             out["attrs:" + g] = np.asarray(json.dumps(a))
         return out
 
+    def _appended(self) -> None:
+        self._pending += 1
+        if self._pending >= self.flush_every:
+            self._flush()
+
+    def close(self) -> None:
+        """Write what is pending (a no-op when every append was flushed)."""
+        if self._pending:
+            self._flush()
+
     def _flush(self) -> None:
+        self._pending = 0
         tmp = self.path + ".tmp.npz"
         with open(tmp, "wb") as fh:
             np.savez(fh, **self._arrays())

@@ -74,3 +74,22 @@ def test_writer_rejects_what_the_reference_rejects(tmp_path):
         w.append_2p2([])  # no 2p2 group in this run
     f = read_results(str(tmp_path / "b.npz"))
     assert f["kernel_sum/x"].shape == (0, 4) and f["attrs:/"]["stride"] == 1
+
+
+def test_flush_every_and_close(tmp_path):
+    from hlbl_gb300.driver import PairResult
+
+    path = str(tmp_path / "c.npz")
+    w = ResultWriter(path, RunInfo(lattice=(4, 4, 4, 4), chains=[Chain()]), flush_every=3)
+    row = PairResult((0, 0, 0, 0), (1, 1, 1, 1), (1, 1, 1, 1), 0, 0, (1.0, 2.0))
+    w.append([row])
+    w.append([row])
+    assert read_results(path)["kernel_sum/x"].shape == (0, 4)  # not yet rewritten
+    w.append([row])
+    assert read_results(path)["kernel_sum/x"].shape == (3, 4)
+    w.append([row])
+    w.close()
+    f = read_results(path)
+    assert f["kernel_sum/kernel_sum"].shape == (4, 2) and f["kernel_sum/kernel_sum"][3, 1] == 2.0
+    with pytest.raises(ValueError):
+        ResultWriter(path, RunInfo(lattice=(4, 4, 4, 4), chains=[Chain()]), flush_every=0)
