@@ -170,6 +170,73 @@ HLBL_QED_HD void hlbl_qed_kernel(const hlbl_qed_params* p, const double x[4],
           kerv[k][mu][nu][lam] = hlbl_qed_entry(w, x, y, k, mu, nu, lam);
 }
 
+/* ---- a second test weight with no closed form ------------------------------
+ *
+ * The stand-in above is a sum of Kronecker structures, and the library's
+ * fast contraction paths exploit that. To check the paths that accept ANY
+ * tensor kerv[6][4][4][4] (a provider with QED_Mkernel_L2's signature), this
+ * dense test weight gives every one of the 384 entries its own seeded
+ * combination of thirteen smooth functions of the two arguments:
+ *
+ *   kerv[i](x, y) = sum_b A[b][i] phi_b(x, y),   i = ((k*4 + mu)*4 + nu)*4 + lam
+ *   phi_0 = g, phi_{1+a} = g x_a, phi_{5+a} = g y_a, phi_{9+a} = g x_a y_a
+ *   g     = 1 / (1 + |x|^2 + |y|^2 + |x - y|^2 / 2)
+ *
+ * with A[b][i] uniform in [-1, 1) from a splitmix64 hash of (seed, b, i)
+ * (exact in binary, the same on every platform). The entries share no
+ * index structure, so no contraction of the tensor has a shortcut. Like the
+ * stand-in it is test physics only. */
+#define HLBL_QED_NK 384       /* entries of kerv[6][4][4][4] */
+#define HLBL_QED_DENSE_NB 13  /* basis functions */
+
+/* A[b][i], row-major: HLBL_QED_DENSE_NB x HLBL_QED_NK doubles. */
+static inline void hlbl_qed_dense_init(double* table, unsigned long long seed) {
+  for (int i = 0; i < HLBL_QED_DENSE_NB * HLBL_QED_NK; ++i) {
+    unsigned long long x = seed * 0x9E3779B97F4A7C15ULL + (unsigned long long)i;
+    x += 0x9E3779B97F4A7C15ULL;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+    x ^= x >> 31;
+    table[i] = (double)(x >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+  }
+}
+
+/* The thirteen basis functions at (x, y). */
+HLBL_QED_HD void hlbl_qed_dense_basis(const double x[4], const double y[4],
+                                      double phi[HLBL_QED_DENSE_NB]) {
+  double xx = 0, yy = 0, dd = 0;
+  for (int a = 0; a < 4; ++a) {
+    double const d = x[a] - y[a];
+    xx += x[a] * x[a];
+    yy += y[a] * y[a];
+    dd += d * d;
+  }
+  double const g = 1.0 / (1.0 + xx + yy + 0.5 * dd);
+  phi[0] = g;
+  for (int a = 0; a < 4; ++a) {
+    phi[1 + a] = g * x[a];
+    phi[5 + a] = g * y[a];
+    phi[9 + a] = g * x[a] * y[a];
+  }
+}
+
+/* Entry i of the tensor from the basis values. */
+HLBL_QED_HD double hlbl_qed_dense_entry(const double* table,
+                                        const double phi[HLBL_QED_DENSE_NB], int i) {
+  double v = 0.0;
+  for (int b = 0; b < HLBL_QED_DENSE_NB; ++b) v += table[b * HLBL_QED_NK + i] * phi[b];
+  return v;
+}
+
+/* The whole tensor, KQED's output layout kerv[6][4][4][4]. */
+HLBL_QED_HD void hlbl_qed_dense_kernel(const double* table, const double x[4],
+                                       const double y[4], double kerv[6][4][4][4]) {
+  double phi[HLBL_QED_DENSE_NB];
+  hlbl_qed_dense_basis(x, y, phi);
+  double* k = &kerv[0][0][0][0];
+  for (int i = 0; i < HLBL_QED_NK; ++i) k[i] = hlbl_qed_dense_entry(table, phi, i);
+}
+
 #ifdef __cplusplus
 }
 #endif

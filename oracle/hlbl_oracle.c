@@ -28,7 +28,9 @@
  * instead of once per inner iteration), which changes no value. Sums over
  * sites use per-thread partials reduced in thread order, so a run is
  * deterministic for a given thread count. The QED kernel is the project's
- * stand-in (include/hlbl_gb300_qed.h), as KQED is not available.
+ * stand-in (include/hlbl_gb300_qed.h), as KQED is not available, or, after
+ * oracle_set_qed_dense, the dense test weight of the same header (a tensor
+ * with no index structure).
  *
  * Parity pin: these functions are checked against the reference's own
  * sources compiled as a host emulation (oracle/ref_host) through the golden
@@ -182,11 +184,31 @@ void oracle_fill_gaussian_block(const int local[4], const int pc[4], uint64_t se
   }
 }
 
-/* ---- the QED kernel (cuda_lattice.cu:266-275 calls QED_Mkernel_L2) ---- */
+/* ---- the QED kernel (cuda_lattice.cu:266-275 calls QED_Mkernel_L2) ----
+ * The stand-in (default) or the dense test weight with a seeded table. */
+static double* g_dense = NULL; /* HLBL_QED_DENSE_NB x HLBL_QED_NK, or NULL */
+
+void oracle_set_qed_dense(int on, unsigned long long seed) {
+  if (!on) {
+    free(g_dense);
+    g_dense = NULL;
+    return;
+  }
+  if (!g_dense) g_dense = (double*)malloc(sizeof(double) * HLBL_QED_DENSE_NB * HLBL_QED_NK);
+  hlbl_qed_dense_init(g_dense, seed);
+}
+int oracle_get_qed_dense(void) { return g_dense != NULL; }
+
+static void qed_kernel(const hlbl_qed_params* p, const double x[4], const double y[4],
+                       double kerv[6][4][4][4]) {
+  if (g_dense) hlbl_qed_dense_kernel(g_dense, x, y, kerv);
+  else hlbl_qed_kernel(p, x, y, kerv);
+}
+
 void oracle_qed_kernel(double lambda, const double x[4], const double y[4], double* kerv) {
   hlbl_qed_params p;
   hlbl_qed_params_init(&p, lambda);
-  hlbl_qed_kernel(&p, x, y, (double(*)[4][4][4])kerv);
+  qed_kernel(&p, x, y, (double(*)[4][4][4])kerv);
 }
 void oracle_qed_weights(double lambda, double X, double c, double Y, double* w) {
   hlbl_qed_params p;
@@ -394,19 +416,19 @@ double oracle_4pt(const double* g_dzu, const double* g_dzsu, const double* fwd_s
       double kerv[6][4][4][4];
       acc_t dtmp = {0.0, 0.0};
       int i;
-      hlbl_qed_kernel(&qp, xm, ym, kerv);
+      qed_kernel(&qp, xm, ym, kerv);
       i = 0;
       for (int k = 0; k < 6; k++)
         for (int mu = 0; mu < 4; mu++)
           for (int nu = 0; nu < 4; nu++)
             for (int lam = 0; lam < 4; lam++) acc_add(&dtmp, kerv[k][mu][nu][lam] * corr_I[i++]);
-      hlbl_qed_kernel(&qp, ym, xm, kerv);
+      qed_kernel(&qp, ym, xm, kerv);
       i = 0;
       for (int k = 0; k < 6; k++)
         for (int mu = 0; mu < 4; mu++)
           for (int nu = 0; nu < 4; nu++)
             for (int lam = 0; lam < 4; lam++) acc_add(&dtmp, kerv[k][nu][mu][lam] * corr_I[i++]);
-      hlbl_qed_kernel(&qp, xm, xm_mi_ym, kerv);
+      qed_kernel(&qp, xm, xm_mi_ym, kerv);
       i = 0;
       for (int k = 0; k < 6; k++)
         for (int mu = 0; mu < 4; mu++)
@@ -563,10 +585,10 @@ void oracle_p234(const double* pi, const int global[4], const int local[4], cons
         }
         const double* P = pi + ix * 16;
         for (int g = 0; g < 4; ++g) {
-          if (g == 0) hlbl_qed_kernel(&qp, xm, ym, kerv);
-          else if (g == 1) hlbl_qed_kernel(&qp, ym, xm, kerv);
-          else if (g == 2) hlbl_qed_kernel(&qp, xmy, ym_minus, kerv);
-          else hlbl_qed_kernel(&qp, ymx, xm_minus, kerv);
+          if (g == 0) qed_kernel(&qp, xm, ym, kerv);
+          else if (g == 1) qed_kernel(&qp, ym, xm, kerv);
+          else if (g == 2) qed_kernel(&qp, xmy, ym_minus, kerv);
+          else qed_kernel(&qp, ymx, xm_minus, kerv);
           for (int k = 0; k < 6; ++k) {
             int const rho = comb[k][0], sigma = comb[k][1];
             for (int nu = 0; nu < 4; ++nu) {

@@ -16,7 +16,10 @@
 #include "hlbl/schedule.hpp"
 #include "hlbl_kernels/kernels.cuh"
 
-// KQED entry points, served by the stand-in weight
+// KQED entry points, served by the stand-in weight or, after
+// ref_set_qed_dense, by the dense test weight (include/hlbl_gb300_qed.h)
+static std::vector<double> g_dense;  // empty: the stand-in
+
 extern "C" int initialise(struct QED_kernel_temps* t) {
   hlbl_qed_params_init(&t->p, 0.4);
   return 0;
@@ -24,9 +27,21 @@ extern "C" int initialise(struct QED_kernel_temps* t) {
 extern "C" int free_QED_temps(struct QED_kernel_temps*) { return 0; }
 extern "C" void QED_Mkernel_L2(const double Lambda, const double xv[4], const double yv[4],
                                const struct QED_kernel_temps t, double kerv[6][4][4][4]) {
+  if (!g_dense.empty()) {
+    hlbl_qed_dense_kernel(g_dense.data(), xv, yv, kerv);
+    return;
+  }
   hlbl_qed_params p = t.p;
   p.lambda = Lambda;
   hlbl_qed_kernel(&p, xv, yv, kerv);
+}
+extern "C" void ref_set_qed_dense(int on, unsigned long long seed) {
+  if (!on) {
+    g_dense.clear();
+    return;
+  }
+  g_dense.assign((std::size_t)HLBL_QED_DENSE_NB * HLBL_QED_NK, 0.0);
+  hlbl_qed_dense_init(g_dense.data(), seed);
 }
 
 namespace {

@@ -101,6 +101,23 @@ CASES = [
 ]
 
 
+def ref_insert_gammas(lib, dzu, dzsu):
+    """g_dzu, g_dzsu from pass 1's sums by the reference's apply_gamma
+    (src/gamma.cpp), in the order of contract.cpp:58-77."""
+    g_dzu, g_dzsu = np.zeros(6912), np.zeros(4608)
+    for src, dst, n in ((dzu, g_dzu, 6), (dzsu, g_dzsu, 4)):
+        for k in range(n):
+            for ia in range(12):
+                for mu in range(4):
+                    t = np.ascontiguousarray(src[(k * 12 + ia) * 24:(k * 12 + ia + 1) * 24])
+                    t5 = np.zeros(24)
+                    lib.ref_apply_gamma(5, vp(t), vp(t5))
+                    o = np.zeros(24)
+                    lib.ref_apply_gamma(mu, vp(t5), vp(o))
+                    dst[((k * 4 + mu) * 12 + ia) * 24:((k * 4 + mu) * 12 + ia + 1) * 24] = o
+    return g_dzu, g_dzsu
+
+
 def inputs(lib, lat, spec):
     if spec[0] == "seeds":
         return ref_block(lib, lat, spec[1]), ref_block(lib, lat, spec[2])
@@ -186,25 +203,7 @@ def main() -> int:
         for f in (0, 1):
             dzu = ranks[0][1][f][0] + ranks[1][1][f][0]
             dzsu = ranks[0][1][f][1] + ranks[1][1][f][1]
-            g_dzu, g_dzsu = np.zeros(6912), np.zeros(4608)
-            for k in range(6):
-                for ia in range(12):
-                    for mu in range(4):
-                        t = dzu[(k * 12 + ia) * 24:(k * 12 + ia + 1) * 24].copy()
-                        t5 = np.zeros(24)
-                        lib.ref_apply_gamma(5, vp(t), vp(t5))
-                        o = np.zeros(24)
-                        lib.ref_apply_gamma(mu, vp(t5), vp(o))
-                        g_dzu[((k * 4 + mu) * 12 + ia) * 24:((k * 4 + mu) * 12 + ia + 1) * 24] = o
-            for s in range(4):
-                for ia in range(12):
-                    for mu in range(4):
-                        t = dzsu[(s * 12 + ia) * 24:(s * 12 + ia + 1) * 24].copy()
-                        t5 = np.zeros(24)
-                        lib.ref_apply_gamma(5, vp(t), vp(t5))
-                        o = np.zeros(24)
-                        lib.ref_apply_gamma(mu, vp(t5), vp(o))
-                        g_dzsu[((s * 4 + mu) * 12 + ia) * 24:((s * 4 + mu) * 12 + ia + 1) * 24] = o
+            g_dzu, g_dzsu = ref_insert_gammas(lib, dzu, dzsu)
             ks = np.zeros(1)
             lib.ref_4pt(vp(ks), vp(g_dzu), vp(g_dzsu), vp(sl[0]), vp(sl[1]), f, i4([r, 0, 0, 0]),
                         i4(gsx2), C.c_double(1.0), i4(yv2), i4(glob), i4(loc))

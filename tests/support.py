@@ -2,6 +2,7 @@
 golden fixtures of tests/golden. Test infrastructure only."""
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 import json
 import os
@@ -65,8 +66,26 @@ def oracle():
         lib.oracle_p234.argtypes = [vpt, I4, I4, I4, I4, vpt, C.c_int, dp, dp, vpt]
         lib.oracle_pieces_2p2.argtypes = [vpt, C.c_int, I4, vpt, C.c_int, dp, dp, I4, I4, I4, vpt,
                                           vpt]
+        lib.oracle_set_qed_dense.argtypes = [C.c_int, C.c_ulonglong]
+        lib.oracle_get_qed_dense.restype = C.c_int
         _oracle = lib
     return _oracle
+
+
+# Seed of the dense test weight (include/hlbl_gb300_qed.h) in every test
+# and fixture that uses it.
+DENSE_SEED = 20261204
+
+
+@contextlib.contextmanager
+def dense_qed(seed=DENSE_SEED):
+    """Within the block the oracle weights with the dense test tensor."""
+    lib = oracle()
+    lib.oracle_set_qed_dense(1, seed)
+    try:
+        yield
+    finally:
+        lib.oracle_set_qed_dense(0, 0)
 
 
 def random_block(local, seed, pc=(0, 0, 0, 0)) -> np.ndarray:
