@@ -88,6 +88,7 @@ def _load() -> C.CDLL:
         "hlbl_surrogate_gradients": (C.c_int, [vp, vp, vp, C.c_int, vp, C.POINTER(C.c_float)]),
         "hlbl_surrogate_eval": (C.c_int, [vp, vp, C.c_int, vp]),
         "hlbl_ctx_set_qed": (C.c_int, [vp, C.c_int, vp, C.c_double]),
+        "hlbl_ctx_set_qed_kernel": (C.c_int, [vp, C.c_int, C.c_uint64]),
         "hlbl_ctx_qed_fallbacks": (C.c_int, [vp, C.POINTER(C.c_ulonglong)]),
         "hlbl_ctx_kernel_times": (C.c_int, [vp, dp, C.POINTER(C.c_longlong)]),
         "hlbl_measure_fma_peak": (C.c_int, [C.c_int, C.c_int, dp]),

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "contract_kernels.cuh"
 #include "hlbl_gb300.h"
@@ -15,6 +16,7 @@
 #include "hlbl_internal.h"
 #include "p2_tc.h"
 #include "pieces_2p2.h"
+#include "qed_provider.cuh"
 
 namespace {
 
@@ -245,6 +247,13 @@ struct hlbl_ctx {
   void* d_bt = nullptr;       // [2][288*160] of double (float uses half of it)
   double* d_w = nullptr;      // QED weights [V][3][6]
   long long w_cap = 0;        // sites d_w holds
+  // the QED kernel (hlbl_ctx_set_qed_kernel): the stand-in's closed form, or
+  // a provider through the generic coefficient path
+  int qed_kind = kQedStandInClosed;
+  double* d_dense64 = nullptr;  // the dense test weight's table [13][384]
+  float* d_dense32 = nullptr;
+  void* d_coef = nullptr;       // generic path: coefficients of a pair group
+  size_t coef_cap = 0;          // bytes of d_coef
   int batch_group = 0;        // pairs per batched launch (0: kMaxBatch)
   int qed_mode = HLBL_QED_EXACT;
   // FP32 path, exact weight: FP32 quadrature outside qed_r64 (FP64 inside)
@@ -396,15 +405,61 @@ int run_weights(hlbl_ctx* c, const Geometry& geo, const PairBatch& b, double xun
   return HLBL_OK;
 }
 
+QedSel qed_sel(const hlbl_ctx* c) {
+  QedSel q;
+  q.kind = c->qed_kind;
+  q.qp = c->qp;
+  q.t64 = c->d_dense64;
+  q.t32 = c->d_dense32;
+  return q;
+}
+
+// Bytes of the generic path's coefficients for n pairs.
+size_t coef_bytes(const Geometry& geo, int n, bool f32) {
+  return (size_t)n * (f32 ? sizeof(float) * coef32_per_pair(geo.V) : sizeof(double) * coef64_per_pair(geo.V));
+}
+
+int ensure_coef(hlbl_ctx* c, size_t need) {
+  if (need <= c->coef_cap) return HLBL_OK;
+  if (c->capturing) return fail(HLBL_ESTATE, "QED coefficient buffer too small during graph capture");
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->d_coef);
+  c->d_coef = nullptr;
+  c->coef_cap = 0;
+  cudaError_t e = cudaMalloc(&c->d_coef, need);
+  if (e != cudaSuccess) return fail(HLBL_ENOMEM, "QED coefficient buffer (%zu bytes): %s", need, cudaGetErrorString(e));
+  c->coef_cap = need;
+  return HLBL_OK;
+}
+
+// The QED weighting of pass 2 for the batch's pairs: the stand-in's weights
+// (closed form) or the generic path's coefficients (FP32 layout for the
+// FP32 path, FP64 layout for the FP64 path), recorded in a.
+int run_qed(hlbl_ctx* c, const Geometry& geo, const PairBatch& b, double xunit, int precision, P2Args& a) {
+  a.w = nullptr;
+  a.coef = nullptr;
+  a.coef_stride = 0;
+  if (c->qed_kind == kQedStandInClosed) {
+    if (int rc = run_weights(c, geo, b, xunit, precision)) return rc;
+    a.w = c->d_w;
+    return HLBL_OK;
+  }
+  bool const f32 = precision == HLBL_FP32;
+  if (int rc = ensure_coef(c, coef_bytes(geo, b.n, f32))) return rc;
+  if (int rc = coef_launch(qed_sel(c), f32, geo, b, xunit, c->d_coef, c->stream)) return rc;
+  a.coef = c->d_coef;
+  a.coef_stride = f32 ? coef32_per_pair(geo.V) : coef64_per_pair(geo.V);
+  return HLBL_OK;
+}
+
 // Pass 2 for the batch's pairs with Bt already built; pair i's sums go to
 // b.p[i].out[0..nf) (added if add).
 int run_pass2(hlbl_ctx* c, const Geometry& geo, const double* y, const PairBatch& b, double xunit,
               int f0, int nf, int precision, int add) {
-  if (int rc = run_weights(c, geo, b, xunit, precision)) return rc;
   P2Args a{};
+  if (int rc = run_qed(c, geo, b, xunit, precision, a)) return rc;
   a.xunit = xunit;
   a.f0 = f0;
-  a.w = c->d_w;
   int grid;
   prof_begin(c, 1);
   if (precision == HLBL_FP64) {
@@ -450,11 +505,10 @@ int run_group_f32(hlbl_ctx* c, const PairBatch& b, const TcBatch& tb, double xun
                                                                              nullptr, nullptr);
   g_build_kernel<<<dim3((kGLen / 2 + 255) / 256, 2, b.n), 256, 0, c->stream>>>(c->d_dz, 2, c->d_g);
   tc_launch_btu(c->d_g, b.n, c->d_btu, c->stream);
-  if (int rc = run_weights(c, geo, b, xunit, HLBL_FP32)) return rc;
   P2Args a{};
+  if (int rc = run_qed(c, geo, b, xunit, HLBL_FP32, a)) return rc;
   a.xunit = xunit;
   a.f0 = 0;
-  a.w = c->d_w;
   int const g2 = per_pair_grid(c->grid_tc, b.n, tc_tiles(geo.V));
   prof_begin(c, 1);
   tc_launch_p2(g2, b.n, c->stream, tb, geo, a, c->d_btu, c->d_part2, c->d_err);
@@ -515,7 +569,8 @@ int hlbl_ctx_create(hlbl_ctx** out, const int global[4], const int local[4],
       (rc = P2D2::init(c->nsm, c->grid_p2d2)) || (rc = P2D1::init(c->nsm, c->grid_p2d1)) ||
       (rc = P2F2::init(c->nsm, c->grid_p2f2)) || (rc = P2F1::init(c->nsm, c->grid_p2f1)) ||
       (rc = P1F2s::init(c->nsm, c->grid_p1f2s)) || (rc = P2F2s::init(c->nsm, c->grid_p2f2s)) ||
-      (rc = tc_init(c->nsm, c->grid_tc)) || (rc = p1f32_init(c->nsm, c->grid_p1f)))
+      (rc = tc_init(c->nsm, c->grid_tc)) || (rc = p1f32_init(c->nsm, c->grid_p1f)) ||
+      (rc = coef_init(c->nsm)))
     return bail(rc);
   c->max_grid = std::max({c->grid_p1d2, c->grid_p1d1, c->grid_p1f2, c->grid_p1f1, c->grid_p2d2,
                           c->grid_p2d1, c->grid_p2f2, c->grid_p2f1, c->grid_p1f2s, c->grid_p2f2s,
@@ -565,6 +620,9 @@ void hlbl_ctx_destroy(hlbl_ctx* c) {
   cudaFree(c->d_out);
   cudaFree(c->d_err);
   cudaFree(c->d_w);
+  cudaFree(c->d_coef);
+  cudaFree(c->d_dense64);
+  cudaFree(c->d_dense32);
   cudaFree(c->d_fallback);
   cudaFree(c->d_p22_out);
   p22_destroy(c->p22);
@@ -634,9 +692,13 @@ int hlbl_kernel_sums_batched_f32(hlbl_ctx* c, const float* y32, int n, const flo
       if (gsx[4 * i + r] < 0 || gsx[4 * i + r] >= c->geo.global[r])
         return fail(HLBL_EINVAL, "hlbl_kernel_sums_batched_f32: gsx of pair %d outside the lattice", i);
   }
-  if (long long need = c->geo.V * std::min(std::max(n, 1), kMaxBatch); need > c->w_cap && c->capturing)
-    return fail(HLBL_ESTATE, "QED weight buffer too small during graph capture");
   int const group = c->group_f32 > 0 ? std::min(c->group_f32, kMaxBatch) : kMaxBatch;
+  if (c->capturing) {
+    bool const small = c->qed_kind == kQedStandInClosed
+                           ? c->geo.V * std::min(std::max(n, 1), kMaxBatch) > c->w_cap
+                           : coef_bytes(c->geo, std::min(std::max(n, 1), group), true) > c->coef_cap;
+    if (small) return fail(HLBL_ESTATE, "QED weight buffer too small during graph capture");
+  }
   for (int i0 = 0; i0 < n; i0 += group) {
     PairBatch b{};
     TcBatch tb{};
@@ -874,7 +936,7 @@ static int p22_launch(hlbl_ctx* c, const double* fwd, int iflavor, const int gsw
   rq.d_p1 = d_p1;
   rq.d_p234 = d_p234;
   rq.raw_layout = raw;
-  if (int rc = p22_run(&c->p22, c->stream, c->geo, c->qp, c->nsm, c->capturing, rq)) return rc;
+  if (int rc = p22_run(&c->p22, c->stream, c->geo, qed_sel(c), c->nsm, c->capturing, rq)) return rc;
   return check_launch("2+2 launch");
 }
 
@@ -968,6 +1030,14 @@ int hlbl_ctx_reserve(hlbl_ctx* c, int max_pairs) {
   if (c->tc) {
     int const group = c->batch_group > 0 ? std::min(c->batch_group, kMaxBatch) : kMaxBatch;
     if (int rc = ensure_x32(c, c->geo, std::min(max_pairs, group))) return rc;
+  }
+  if (c->qed_kind != kQedStandInClosed) {
+    // the generic path's coefficients: FP64 layout for the pair groups of the
+    // FP64-block calls, FP32 layout for those of the FP32-copy path
+    int const g64 = c->batch_group > 0 ? std::min(c->batch_group, kMaxBatch) : kMaxBatch;
+    int const g32 = c->group_f32 > 0 ? std::min(c->group_f32, kMaxBatch) : kMaxBatch;
+    return ensure_coef(c, std::max(coef_bytes(c->geo, std::min(max_pairs, g64), false),
+                                   coef_bytes(c->geo, std::min(max_pairs, g32), true)));
   }
   long long const need = c->geo.V * std::min(max_pairs, kMaxBatch);
   if (need <= c->w_cap) return HLBL_OK;
@@ -1097,8 +1167,36 @@ void hlbl_graph_destroy(hlbl_graph* g) {
   delete g;
 }
 
+int hlbl_ctx_set_qed_kernel(hlbl_ctx* c, int kind, uint64_t seed) {
+  if (!c) return fail(HLBL_EINVAL, "hlbl_ctx_set_qed_kernel: null context");
+  if (kind < 0 || kind >= kQedKinds) return fail(HLBL_EINVAL, "hlbl_ctx_set_qed_kernel: bad kind %d", kind);
+  if (c->capturing) return fail(HLBL_ESTATE, "hlbl_ctx_set_qed_kernel: during graph capture");
+  if (kind != kQedStandInClosed && c->qed_mode == HLBL_QED_SURROGATE)
+    return fail(HLBL_ESTATE, "hlbl_ctx_set_qed_kernel: the learned weight replaces the stand-in's closed form only");
+  if (kind == kQedDense || kind == kQedDenseKerv) {
+    std::vector<double> t64((size_t)HLBL_QED_DENSE_NB * HLBL_QED_NK);
+    hlbl_qed_dense_init(t64.data(), (unsigned long long)seed);
+    std::vector<float> t32(t64.size());
+    for (size_t i = 0; i < t64.size(); ++i) t32[i] = (float)t64[i];
+    cudaError_t e = cudaSuccess;
+    if (!c->d_dense64) e = cudaMalloc(&c->d_dense64, sizeof(double) * t64.size());
+    if (e == cudaSuccess && !c->d_dense32) e = cudaMalloc(&c->d_dense32, sizeof(float) * t32.size());
+    if (e != cudaSuccess) return fail(HLBL_ENOMEM, "hlbl_ctx_set_qed_kernel: %s", cudaGetErrorString(e));
+    // ordered on the context's stream after every launch that reads the old table
+    e = cudaMemcpyAsync(c->d_dense64, t64.data(), sizeof(double) * t64.size(), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(c->d_dense32, t32.data(), sizeof(float) * t32.size(), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "hlbl_ctx_set_qed_kernel: table upload");
+  }
+  c->qed_kind = kind;
+  return HLBL_OK;
+}
+
 int hlbl_ctx_set_qed(hlbl_ctx* c, int mode, hlbl_surrogate* s, double r0) {
   if (!c) return fail(HLBL_EINVAL, "hlbl_ctx_set_qed: null context");
+  if (mode == HLBL_QED_SURROGATE && c->qed_kind != kQedStandInClosed)
+    return fail(HLBL_ESTATE, "hlbl_ctx_set_qed: the learned weight replaces the stand-in's closed form only");
   if (mode == HLBL_QED_EXACT) {
     c->qed_mode = mode;
     c->sur = nullptr;

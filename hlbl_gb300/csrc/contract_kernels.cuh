@@ -645,10 +645,32 @@ static __global__ void qed_weights_fp32_kernel(Geometry geo, WArgs args, double 
   }
 }
 
+// Coefficient layouts in HBM of the generic QED path (qed_provider.cuh), per
+// pair:
+//   FP64 (the FP64 pass 2): [V][4][160] doubles, a site's 640 contiguous;
+//   FP32 (the tensor-core and CUDA-core FP32 pass 2): tiles of 32 sites,
+//     [tile][mu][n/4][32 sites][4] floats, so that the 32 rows (mu, site) of
+//     one TMEM lane quadrant read 512 contiguous bytes per group of four n;
+//     the last tile is padded with zeros.
+constexpr int kCoefPerSite = 4 * kBtN;  // 640
+__host__ __device__ __forceinline__ size_t coef32_index(long long site, int mu, int n) {
+  long long const tile = site >> 5;
+  return ((((size_t)tile * 4 + mu) * (kBtN / 4) + (n >> 2)) * 32 + (size_t)(site & 31)) * 4 + (n & 3);
+}
+__host__ __device__ __forceinline__ size_t coef32_per_pair(long long V) {
+  return (size_t)((V + 31) / 32) * 32 * kCoefPerSite;
+}
+__host__ __device__ __forceinline__ size_t coef64_per_pair(long long V) {
+  return (size_t)V * kCoefPerSite;
+}
+
 struct P2Args {
   double xunit;
   int f0;                 // first flavour
-  const double* w;        // QED weights [pair][V][3][6] (qed_weights_*_kernel)
+  const double* w;        // QED weights [pair][V][3][6] (qed_weights_*_kernel), closed form
+  const void* coef;       // or (generic QED path) the coefficients, T of the kernel, in the
+                          // FP64 layout for T = double and the FP32 layout for T = float
+  size_t coef_stride;     // elements per pair of coef
 };
 
 template <typename T, int NF, int TS>
@@ -692,7 +714,7 @@ p2_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, P2Args ar
   const double* __restrict__ src = batch.p[pi].src;
   int const gsx[4] = {batch.p[pi].gsx[0], batch.p[pi].gsx[1], batch.p[pi].gsx[2], batch.p[pi].gsx[3]};
   int const yv[4] = {batch.p[pi].yv[0], batch.p[pi].yv[1], batch.p[pi].yv[2], batch.p[pi].yv[3]};
-  const double* __restrict__ wq = args.w + (size_t)pi * geo.V * 3 * HLBL_QED_NW;
+  const double* __restrict__ wq = args.w ? args.w + (size_t)pi * geo.V * 3 * HLBL_QED_NW : nullptr;
   const T* __restrict__ bt = bt_all + (size_t)pi * NF * kBtK * kBtN;
   double const xu = args.xunit;
   double ym[4];
@@ -740,6 +762,20 @@ p2_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, P2Args ar
       s_vec[s * 12 + 8 + r] = (double)coord_map_zerohalf(rel[r], geo.global[r]);
     }
     __syncthreads();
+    if (args.coef) {
+      // generic QED path: the coefficients of the tile's sites (zero past the end)
+      const T* cg = static_cast<const T*>(args.coef) + (size_t)pi * args.coef_stride;
+      for (int it = t; it < TS * kCoefPerSite; it += nthr) {
+        int const s = it / kCoefPerSite, mn = it % kCoefPerSite;
+        long long const site = s0 + s;
+        T v = T(0);
+        if (site < geo.V) {
+          if constexpr (sizeof(T) == 8) v = __ldg(cg + (size_t)site * kCoefPerSite + mn);
+          else v = __ldg(cg + coef32_index(site, mn / kBtN, mn % kBtN));
+        }
+        s_coef[it] = v;
+      }
+    } else {
     // the QED tensor's inputs per (site, evaluation), in T:
     // e = 0: K(x, y), e = 1: K(y, x), e = 2: K(x, x - y)
     for (int it = t; it < TS * 3 * kQ; it += nthr) {
@@ -776,6 +812,7 @@ p2_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, P2Args ar
         }
       }
       s_coef[(s * 4 + mu) * kBtN + n] = (s0 + s < geo.V) ? cf : T(0);
+    }
     }
     // the tile's blocks
     uint32_t const parity = kDB ? (uint32_t)((it_tile >> 1) & 1) : (uint32_t)(it_tile & 1);

@@ -309,7 +309,40 @@ __device__ __forceinline__ float epilogue_row(uint32_t lane_addr, uint32_t c, co
   return a;
 }
 
+// Generic QED path: one phase's row dotted with the row's coefficients,
+// read from the FP32 coefficient layout (crow: this row's (tile, mu, site)
+// base; group g of four n at crow + g*128), one 16-column block of F per j.
+// The next block's coefficients are loaded while the current one is dotted.
+__device__ __forceinline__ float epilogue_row_generic(uint32_t lane_addr, uint32_t c, const float* crow) {
+  float f[16], a = 0.f;
+  float4 cf[4], cn[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) cf[i] = __ldg(reinterpret_cast<const float4*>(crow + i * 128));
+#pragma unroll 1
+  for (int jj = 0; jj < 10; ++jj) {
+    if (jj + 1 < 10) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) cn[i] = __ldg(reinterpret_cast<const float4*>(crow + ((jj + 1) * 4 + i) * 128));
+    }
+    tmem_ld16(lane_addr + c + 16 * jj, f);
+    tmem_wait_ld();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      a = fmaf(cf[i].x, f[4 * i], a);
+      a = fmaf(cf[i].y, f[4 * i + 1], a);
+      a = fmaf(cf[i].z, f[4 * i + 2], a);
+      a = fmaf(cf[i].w, f[4 * i + 3], a);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) cf[i] = cn[i];
+  }
+  return a;
+}
+
 // ---- the kernel ------------------------------------------------------------------
+// kGeneric: the QED weighting from the coefficient tensor of args.coef (any
+// QED kernel, qed_provider.cuh) instead of the stand-in's closed form.
+template <bool kGeneric>
 __global__ void __launch_bounds__(kThreads, 1)
 p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu,
             double* __restrict__ partials, int* __restrict__ err) {
@@ -570,7 +603,9 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
     uint32_t const lane_addr = tmem + ((uint32_t)(quad * 32) << 16);
     const int gsx[4] = {tb.gsx[pi][0], tb.gsx[pi][1], tb.gsx[pi][2], tb.gsx[pi][3]};
     const int yv[4] = {tb.yv[pi][0], tb.yv[pi][1], tb.yv[pi][2], tb.yv[pi][3]};
-    const double* __restrict__ wq = args.w + (size_t)pi * geo.V * 3 * HLBL_QED_NW;
+    const double* __restrict__ wq = kGeneric ? nullptr : args.w + (size_t)pi * geo.V * 3 * HLBL_QED_NW;
+    const float* __restrict__ cg =
+        kGeneric ? static_cast<const float*>(args.coef) + (size_t)pi * args.coef_stride : nullptr;
     double const xu = args.xunit;
     SiteQ q;
 #pragma unroll
@@ -580,7 +615,7 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
       long long const tile = blockIdx.x + (long long)(P >> 1) * gridDim.x;
       long long const v = tile * kSites + s;
       bool const valid = v < geo.V;
-      if ((P & 1) == 0) {
+      if (!kGeneric && (P & 1) == 0) {
         // the row's site data, for both flavours of the tile
         long long const vv = valid ? v : geo.V - 1;
         int rel[4];
@@ -617,11 +652,16 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
       if (lane == 0) mbar_arrive(&sm.folded);
       tc_fence_after();
       float a;
-      switch (quad) {
-        case 0: a = epilogue_row<0>(lane_addr, c0, q); break;
-        case 1: a = epilogue_row<1>(lane_addr, c0, q); break;
-        case 2: a = epilogue_row<2>(lane_addr, c0, q); break;
-        default: a = epilogue_row<3>(lane_addr, c0, q); break;
+      if constexpr (kGeneric) {
+        // the row (mu = quad, site s of the tile); pad sites' coefficients are zero
+        a = epilogue_row_generic(lane_addr, c0, cg + coef32_index(tile * kSites, quad, 0) + (size_t)s * 4);
+      } else {
+        switch (quad) {
+          case 0: a = epilogue_row<0>(lane_addr, c0, q); break;
+          case 1: a = epilogue_row<1>(lane_addr, c0, q); break;
+          case 2: a = epilogue_row<2>(lane_addr, c0, q); break;
+          default: a = epilogue_row<3>(lane_addr, c0, q); break;
+        }
       }
       tc_fence_before();
       __syncwarp();
@@ -726,13 +766,18 @@ int tc_threads() { return tc::kThreads; }
 size_t tc_btu_floats_per_pair() { return (size_t)2 * tc::kChunks * 2 * tc::kBPart; }
 
 int tc_init(int nsm, int& grid) {
-  cudaError_t e = cudaFuncSetAttribute(tc::p2tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(tc::p2tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)sizeof(tc::Smem));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(tc::p2tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(tc::Smem));
   if (e != cudaSuccess) return cuda_fail(e, "p2tc smem attribute");
-  int nb = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tc::p2tc_kernel, tc::kThreads, sizeof(tc::Smem));
+  int nb = 0, nbg = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tc::p2tc_kernel<false>, tc::kThreads, sizeof(tc::Smem));
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbg, tc::p2tc_kernel<true>, tc::kThreads, sizeof(tc::Smem));
   if (e != cudaSuccess) return cuda_fail(e, "p2tc occupancy");
-  if (nb < 1) return fail(HLBL_ECUDA, "p2tc kernel cannot be resident (smem %zu)", sizeof(tc::Smem));
+  if (nb < 1 || nbg < 1) return fail(HLBL_ECUDA, "p2tc kernel cannot be resident (smem %zu)", sizeof(tc::Smem));
   // one CTA per SM: each allocates all 512 TMEM columns
   grid = nsm;
   return HLBL_OK;
@@ -745,7 +790,10 @@ void tc_launch_btu(const double* d_g, int npairs, float* d_btu, cudaStream_t st)
 
 void tc_launch_p2(int grid, int npairs, cudaStream_t st, const TcBatch& tb, const Geometry& geo,
                   const P2Args& a, const float* d_btu, double* partials, int* err) {
-  tc::p2tc_kernel<<<dim3(grid, npairs), tc::kThreads, sizeof(tc::Smem), st>>>(tb, geo, a, d_btu, partials, err);
+  if (a.coef)
+    tc::p2tc_kernel<true><<<dim3(grid, npairs), tc::kThreads, sizeof(tc::Smem), st>>>(tb, geo, a, d_btu, partials, err);
+  else
+    tc::p2tc_kernel<false><<<dim3(grid, npairs), tc::kThreads, sizeof(tc::Smem), st>>>(tb, geo, a, d_btu, partials, err);
 }
 
 long long tc_tiles(long long V) { return (V + tc::kSites - 1) / tc::kSites; }

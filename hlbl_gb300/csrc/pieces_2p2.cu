@@ -46,6 +46,7 @@
 #include "hlbl_internal.h"
 #include "pieces_2p2.h"
 #include "qed_f32.cuh"
+#include "qed_provider.cuh"
 
 namespace hg {
 namespace p22 {
@@ -360,13 +361,54 @@ __device__ __forceinline__ void weights(const P234Args& p, const T* a, const T* 
 // (r, s) with r < s -> k
 __host__ __device__ constexpr int comb_index(int r, int s) { return r == 0 ? s - 1 : (r == 1 ? s + 1 : 5); }
 
+// The stand-in's closed-form contraction (the fast variant; contract above).
+struct ClosedStandIn {};
+
+// Geometry G's contraction of ANY QED kernel (a provider, qed_provider.cuh)
+// with Pi, entry by entry (kernel_p20/p21/p3/p4's index order,
+// kernels.cu:374-750), the kept index f:
+//   G = 0: v[k][f] = sum_{m,l} K[k][m][f][l] P[m][l]   (P2_0)
+//   G = 1: v[k][f] = sum_{n,l} K[k][f][n][l] P[n][l]   (P2_1)
+//   G = 2: v[k][f] = sum_{m,n} K[k][m][n][f] P[m][n]   (P3)
+//   G = 3: v[k][f] = sum_{n,l} K[k][f][n][l] P[l][n]   (P4)
+// 384 entries per evaluation.
+template <typename T, int G, class Q>
+__device__ __forceinline__ void generic_contract(const Q& prov, const T* a, const T* b, const T* P, T* v) {
+  double ad[4], bd[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    ad[r] = (double)a[r];
+    bd[r] = (double)b[r];
+  }
+  T st[Q::kState];
+  prov.template prepare<T>(ad, bd, st);
+  for (int k = 0; k < 6; ++k) {
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+      T acc = T(0);
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          int const idx = G == 0 ? kerv_index(k, i, f, j)
+                        : G == 2 ? kerv_index(k, i, j, f)
+                                 : kerv_index(k, f, i, j);
+          T const m = G == 3 ? P[j * 4 + i] : P[i * 4 + j];
+          acc = fma(prov.template entry<T>(st, idx), m, acc);
+        }
+      v[k * 4 + f] = acc;
+    }
+  }
+}
+
 // Geometry G of every target of the launch, partial sums of this CTA:
 // part[((t * 5 + slot) * pstride + blockIdx.x) * 64 + rho*16 + sigma*4 + nu].
 // FP32: four CTAs per SM (three for G = 3 and its 72 sums); FP64: as many as fit
-template <typename T, int G>
+// Q: ClosedStandIn (the stand-in's closed form, the weights from p.qp) or a
+// provider (any QED kernel, generic_contract).
+template <typename T, int G, class Q>
 __global__ void __launch_bounds__(kP234Threads, sizeof(T) == 4 ? (G == 3 ? 3 : 4) : 1)
-    p234_kernel(P234Args p, const T* __restrict__ rec,
-                                                            int pstride, double* __restrict__ part) {
+    p234_kernel(P234Args p, Q prov, const T* __restrict__ rec, int pstride, double* __restrict__ part) {
   constexpr int NA = G == 3 ? 72 : 24;
   constexpr int NW = kP234Threads / 32;
   __shared__ double red[NW][NA];
@@ -434,12 +476,17 @@ __global__ void __launch_bounds__(kP234Threads, sizeof(T) == 4 ? (G == 3 ? 3 : 4
           b[r] = wrap(-xv[r], r) * xu;
         }
       }
-    T w[6], v[24];
-      weights<T>(p, a, b, w);
-      if constexpr (G == 0) contract<T, 2, false>(a, b, w, P, v);
-      else if constexpr (G == 1) contract<T, 1, false>(a, b, w, P, v);
-      else if constexpr (G == 2) contract<T, 3, false>(a, b, w, P, v);
-      else contract<T, 1, true>(a, b, w, P, v);
+      T v[24];
+      if constexpr (std::is_same_v<Q, ClosedStandIn>) {
+        T w[6];
+        weights<T>(p, a, b, w);
+        if constexpr (G == 0) contract<T, 2, false>(a, b, w, P, v);
+        else if constexpr (G == 1) contract<T, 1, false>(a, b, w, P, v);
+        else if constexpr (G == 2) contract<T, 3, false>(a, b, w, P, v);
+        else contract<T, 1, true>(a, b, w, P, v);
+      } else {
+        generic_contract<T, G, Q>(prov, a, b, P, v);
+      }
 #pragma unroll
       for (int i = 0; i < 24; ++i) acc[i] += v[i];
       if constexpr (G == 3) {
@@ -530,7 +577,8 @@ namespace {
 template <typename T, int G>
 int grid_of(int nsm, int& grid) {
   int nb = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, p234_kernel<T, G>, kP234Threads, 0);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, p234_kernel<T, G, ClosedStandIn>,
+                                                                kP234Threads, 0);
   if (e != cudaSuccess) return cuda_fail(e, "2+2 occupancy");
   if (nb < 1) return fail(HLBL_ECUDA, "2+2 kernel cannot be resident");
   grid = nsm * (nb < 8 ? nb : 8);
@@ -590,8 +638,24 @@ int p22_lmax(const Geometry& geo) {
   return l;
 }
 
+// The four per-target kernels of one chunk of targets; generic providers
+// run every geometry on the partials' full CTA stride (their sums do not
+// depend on the grid).
+template <typename T, class Q>
+static SlotCtas launch_p234(P22* s, cudaStream_t st, const P234Args& args, const Q& prov, const T* pi) {
+  const int* gc = s->grid_p234[sizeof(T) == 4 ? 1 : 0];
+  int g[4];
+  for (int i = 0; i < 4; ++i) g[i] = std::is_same_v<Q, ClosedStandIn> ? gc[i] : s->pstride;
+  p234_kernel<T, 0, Q><<<g[0], kP234Threads, 0, st>>>(args, prov, pi, s->pstride, s->d_part);
+  p234_kernel<T, 1, Q><<<g[1], kP234Threads, 0, st>>>(args, prov, pi, s->pstride, s->d_part);
+  p234_kernel<T, 2, Q><<<g[2], kP234Threads, 0, st>>>(args, prov, pi, s->pstride, s->d_part);
+  p234_kernel<T, 3, Q><<<g[3], kP234Threads, 0, st>>>(args, prov, pi, s->pstride, s->d_part);
+  return SlotCtas{{g[0], g[1], g[2], g[3], g[3]}};
+}
+
 template <typename T>
-static void launch_all(P22* s, cudaStream_t st, const Geometry& geo, const P22Request& rq, P234Args& args) {
+static void launch_all(P22* s, cudaStream_t st, const Geometry& geo, const P22Request& rq, P234Args& args,
+                       const QedSel& q) {
   T* pi = reinterpret_cast<T*>(s->d_pi);
   int4 const gsw = make_int4(rq.gsw[0], rq.gsw[1], rq.gsw[2], rq.gsw[3]);
   long long const ntiles = (geo.V + kPiSites - 1) / kPiSites;
@@ -614,18 +678,18 @@ static void launch_all(P22* s, cudaStream_t st, const Geometry& geo, const P22Re
     for (int t = 0; t < nt; ++t)
       for (int r = 0; r < 4; ++r)
         args.y[t][r] = mod_pos(rq.targets[4 * (t0 + t) + r] - rq.gsw[r], geo.global[r]);
-    const int* g = s->grid_p234[sizeof(T) == 4 ? 1 : 0];
-    p234_kernel<T, 0><<<g[0], kP234Threads, 0, st>>>(args, pi, s->pstride, s->d_part);
-    p234_kernel<T, 1><<<g[1], kP234Threads, 0, st>>>(args, pi, s->pstride, s->d_part);
-    p234_kernel<T, 2><<<g[2], kP234Threads, 0, st>>>(args, pi, s->pstride, s->d_part);
-    p234_kernel<T, 3><<<g[3], kP234Threads, 0, st>>>(args, pi, s->pstride, s->d_part);
-    SlotCtas const n{{g[0], g[1], g[2], g[3], g[3]}};
+    SlotCtas n;
+    if (q.kind == kQedStandInClosed)
+      n = launch_p234<T>(s, st, args, ClosedStandIn{}, pi);
+    else
+      n = with_provider(q, [&](auto prov) { return launch_p234<T>(s, st, args, prov, pi); });
     p234_reduce_kernel<<<nt * 5, 64 * kRedGroups, 0, st>>>(s->d_part, s->pstride, n, rq.n_y, t0, rq.raw_layout, rq.d_p234);
   }
 }
 
-int p22_run(P22** st, cudaStream_t stream, const Geometry& geo, const hlbl_qed_params& qp, int nsm,
+int p22_run(P22** st, cudaStream_t stream, const Geometry& geo, const QedSel& q, int nsm,
             bool capturing, const P22Request& rq) {
+  hlbl_qed_params const& qp = q.qp;
   if (!*st || (*st)->V < geo.V || !(*st)->d_pi) {
     if (capturing) return fail(HLBL_ESTATE, "2+2: work buffers not reserved before graph capture");
     if (int rc = p22_reserve(st, geo, nsm)) return rc;
@@ -641,8 +705,8 @@ int p22_run(P22** st, cudaStream_t stream, const Geometry& geo, const hlbl_qed_p
   args.qp = qp;
   args.r64f = (float)rq.r64;
   qed_f32_tables(qp, args.qf);
-  if (rq.precision == HLBL_FP64) launch_all<double>(s, stream, geo, rq, args);
-  else launch_all<float>(s, stream, geo, rq, args);
+  if (rq.precision == HLBL_FP64) launch_all<double>(s, stream, geo, rq, args, q);
+  else launch_all<float>(s, stream, geo, rq, args, q);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "2+2 launch");
   return HLBL_OK;

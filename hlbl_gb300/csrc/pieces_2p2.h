@@ -40,7 +40,8 @@ struct P22Request {
 
 struct P22;
 int p22_reserve(P22** st, const Geometry& geo, int nsm);
-int p22_run(P22** st, cudaStream_t stream, const Geometry& geo, const hlbl_qed_params& qp, int nsm,
+struct QedSel;
+int p22_run(P22** st, cudaStream_t stream, const Geometry& geo, const QedSel& q, int nsm,
             bool capturing, const P22Request& rq);
 void p22_destroy(P22* st);
 int p22_lmax(const Geometry& geo);

@@ -203,14 +203,17 @@ int hlbl_cu_4pt_contraction(hlbl_ctx* ctx, double* d_kernel_sum, const double* d
  * one that measures free memory around the kernels. It needs no context and
  * allocates nothing. Its scratch (per-thread-block partial sums) is a fixed
  * array of HLBL_NOALLOC_MAX_BLOCKS x 2880 doubles (11.8 MB) in the library's
- * device image, held on every GPU that loads the library until exit; a call
- * whose pass 1 would run more thread blocks than that fails with
- * HLBL_EINVAL. Runs on `stream` (a cudaStream_t; NULL = legacy default) on
- * the current device. The first call on a device looks up the array's device
- * address and the kernel's occupancy, so make that first call before any
- * stream capture. All calls share the array: calls that overlap on the GPU
- * (other streams, other host threads) race and give wrong sums; order them.
- * No counterpart in the reference. */
+ * device image, held on every GPU that loads the library until exit; pass 1
+ * walks the lattice's tiles with at most that many thread blocks, so every
+ * lattice size fits. Runs on `stream` (a cudaStream_t; NULL = legacy
+ * default) on the current device. The first call on a device looks up the
+ * array's device address and the kernel's occupancy, so make that first call
+ * before any stream capture. If a thread block gives up its bounded wait for
+ * a staged tile, every element added into d_dzu and d_dzsu is NaN (the call
+ * itself has returned HLBL_OK by then). All calls share the array and its
+ * error word: calls that overlap on the GPU (other streams, other host
+ * threads) race and give wrong sums; order them. No counterpart in the
+ * reference. */
 #define HLBL_NOALLOC_MAX_BLOCKS 512
 int hlbl_cu_dzu_dzsu_noalloc(double* d_dzu, double* d_dzsu, const double* fwd_src,
                              const double* fwd_y, int iflavor, const int proc_coords[4],
@@ -326,6 +329,29 @@ int hlbl_surrogate_gradients(hlbl_surrogate* s, const float* feat, const float* 
                              float* grad, float* loss);
 /* The inference kernel's raw network outputs for host rows feat[n][3]. */
 int hlbl_surrogate_eval(hlbl_surrogate* s, const float* feat, int n, float* out);
+/* ---- the QED kernel ------------------------------------------------------
+ * Which QED kernel pass 2 and the 2+2 pieces weight with. KQED's
+ * QED_Mkernel_L2 (kernels/cuda_lattice.cu:266-275, kernels.cu:238) is not
+ * available, so the library carries two test kernels with its signature
+ * (include/hlbl_gb300_qed.h):
+ *   HLBL_QEDK_STANDIN          the stand-in through its closed-form fast
+ *                              paths (the default)
+ *   HLBL_QEDK_STANDIN_GENERIC  the same tensor through the generic paths
+ *   HLBL_QEDK_DENSE            the dense test weight (no index structure,
+ *                              table seeded by `seed`), generic paths, entry
+ *                              by entry
+ *   HLBL_QEDK_DENSE_KERV       the same tensor evaluated whole per call, as
+ *                              a QED_Mkernel_L2-shaped function is
+ * The generic paths use no structure of the tensor: a coefficient stage
+ * folds the three evaluations per site into 640 coefficients in HBM (FP32
+ * or FP64 by the path), which the contraction kernels dot with their F rows,
+ * and the 2+2 kernels contract all 384 entries per evaluation. The learned
+ * weight (hlbl_ctx_set_qed) replaces the stand-in's closed form only.
+ * Blocking. No counterpart in the reference (it links one kernel). */
+enum { HLBL_QEDK_STANDIN = 0, HLBL_QEDK_STANDIN_GENERIC = 1, HLBL_QEDK_DENSE = 2,
+       HLBL_QEDK_DENSE_KERV = 3 };
+int hlbl_ctx_set_qed_kernel(hlbl_ctx* ctx, int kind, uint64_t seed);
+
 /* Pass 2's QED weight: HLBL_QED_EXACT, or HLBL_QED_SURROGATE with `s` and
  * fallback radius r0 (r0 < 0: the radius the training validation chose). */
 int hlbl_ctx_set_qed(hlbl_ctx* ctx, int mode, hlbl_surrogate* s, double r0);

@@ -4,9 +4,11 @@ It serves callers that cannot allocate device memory when they contract --
 a process whose solver already holds nearly all device memory in its own
 pool, or one measuring free memory around the kernels. Its scratch is a
 fixed array inside the library that every call reuses, so this test calls
-it twice in a row with different inputs and checks each result against the
-context-based entry point, hlbl_cu_dzu_dzsu, at the FP64 bar of the other
-parity tests (1e-12 relative). The file is named to be collected last.
+it several times in a row with different inputs and checks each result
+against the context-based entry point, hlbl_cu_dzu_dzsu, and against the CPU
+oracle, at the FP64 bar of the other parity tests (1e-12 relative). One case
+has far more tiles than thread blocks (each block walks many tiles, with the
+next tile's copy in flight). The file is named to be collected last.
 """
 import ctypes as C
 
@@ -51,12 +53,18 @@ def test_noalloc_pass1_matches_context_entry_twice_in_a_row():
         # (lattice, local, proc coords, seeds, flavour, gsx)
         ((8, 6, 6, 6), (8, 6, 6, 6), (0, 0, 0, 0), (41, 42), 0, (3, 1, 5, 2)),
         ((8, 4, 4, 4), (4, 4, 4, 4), (1, 0, 0, 0), (43, 44), 1, (6, 0, 3, 1)),
+        # 8,192 tiles of 8 sites: many more than the resident blocks
+        ((16, 16, 16, 16), (16, 16, 16, 16), (0, 0, 0, 0), (45, 46), 1, (9, 2, 15, 7)),
     ]
     for glob, loc, pc, seeds, f, gsx in cases:
-        src = torch.from_numpy(S.random_block(loc, seeds[0], pc)).cuda()
-        y = torch.from_numpy(S.random_block(loc, seeds[1], pc)).cuda()
+        h_src, h_y = S.random_block(loc, seeds[0], pc), S.random_block(loc, seeds[1], pc)
+        src, y = torch.from_numpy(h_src).cuda(), torch.from_numpy(h_y).cuda()
         want = _with_context(hg, src, y, f, gsx, glob, loc, pc)
+        dzu, dzsu = S.oracle_dz(h_src, h_y, f, gsx, glob, loc, pc)
+        oracle = np.concatenate([np.ravel(dzu), np.ravel(dzsu)])
         got = _without_allocation(lib, src, y, f, gsx, glob, loc, pc)
+        assert np.all(np.isfinite(got))
         scale = np.max(np.abs(want))
         assert scale > 0
         assert np.max(np.abs(got - want)) <= TOL64 * scale
+        assert np.max(np.abs(got - oracle)) <= TOL64 * np.max(np.abs(oracle))
