@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip the baseline leg of the reference's own kernels on the GPU")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default kernel variants (profiling: the first launches are the timed ones)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -716,12 +718,91 @@ def main():
                                "sample": f"one pair, pass 1 + pass 2 both flavours over {ns} of 48 "
                                          f"time slices, scaled by 48/{ns}; plain FP64 loops of the "
                                          f"reference restated in C (oracle), OpenMP"}
+    if rank == 0 and not args.no_reference_gpu:
+        p, qs = timed[0]
+        q = qs[0]
+        out["reference_gpu_baseline"] = reference_gpu_baseline(
+            torch, c, hg, block(q), block(p), schedule.mod_pos(q, LATTICE), schedule.site_map_diff(p, q, LATTICE),
+            xu, res64[0].cpu().tolist(), res_main[0].cpu().tolist(), schedule.mod_pos(p, LATTICE))
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+def reference_gpu_baseline(torch, c, hg, d_src, d_y, gsx, yv, xu, ours64, ours32, gsw):
+    """Baseline leg: the reference's OWN Contractor and kernels
+    (kernels/cuda_lattice.cu, kernels/hlbl_kernels/kernels.cu, src/contract.cpp),
+    built for sm_103a by the committed recipe oracle/ref_gpu with the stand-in
+    QED weight on the device, timed on this GPU: one pair (both flavours,
+    Contractor::kernel_sum, which blocks on its host round trips) and one
+    source's 2+2 pieces for the same targets as the pieces_2p2 line. The
+    library's results for the same inputs are compared with it."""
+    import platform
+
+    import numpy as np
+
+    path = os.path.join(ROOT, "oracle", "_ref", "gpu", platform.machine(), "libhlbl_ref_gpu.so")
+    if not os.path.exists(path):
+        return {"unavailable": "the reference's GPU build (oracle/_ref/gpu) is absent: no staged copy of its sources"}
+    lib = C.CDLL(path)
+    I4 = C.c_int * 4
+    vpt = C.c_void_p
+    lib.refgpu_last_error.restype = C.c_char_p
+    lib.refgpu_create.argtypes = [C.POINTER(vpt), I4, C.c_int, C.c_ulonglong]
+    lib.refgpu_destroy.argtypes = [vpt]
+    lib.refgpu_kernel_sum.argtypes = [vpt, vpt, vpt, I4, I4, C.c_double, vpt]
+    lib.refgpu_pieces_2p2.argtypes = [vpt, vpt, I4, vpt, C.c_int, C.c_double, vpt, vpt]
+    lib.refgpu_reserve_kernel_memory.argtypes = [vpt, C.c_int, C.POINTER(C.c_size_t)]
+    h = vpt()
+    if lib.refgpu_create(C.byref(h), I4(*LATTICE), 0, 0) != 0:
+        return {"unavailable": "refgpu_create: " + lib.refgpu_last_error().decode()}
+    try:
+        nb = C.c_size_t()
+        torch.cuda.synchronize()
+        # the reference's own preflight: the first launches reserve the kernels' stack
+        if lib.refgpu_reserve_kernel_memory(h, 1, C.byref(nb)) != 0:
+            return {"unavailable": "reserve_kernel_memory: " + lib.refgpu_last_error().decode()}
+        ks = (C.c_double * 2)()
+        t0 = time.perf_counter()
+        rc = lib.refgpu_kernel_sum(h, vpt(d_src.data_ptr()), vpt(d_y.data_ptr()), I4(*gsx), I4(*yv),
+                                   C.c_double(xu), ks)
+        t_pair = time.perf_counter() - t0
+        if rc != 0:
+            return {"unavailable": "kernel_sum: " + lib.refgpu_last_error().decode()}
+        ref = np.array([ks[0], ks[1]])
+        targets = targets_2p2(gsw, N_TARGETS_2P2)
+        tg = np.ascontiguousarray(np.asarray(targets, dtype=np.int32))
+        p1 = np.zeros(64 * max(LATTICE))
+        p234 = np.zeros(N_TARGETS_2P2 * 320)
+        t0 = time.perf_counter()
+        rc = lib.refgpu_pieces_2p2(h, vpt(d_y.data_ptr()), I4(*gsw), tg.ctypes.data_as(vpt), len(targets),
+                                   C.c_double(xu), p1.ctypes.data_as(vpt), p234.ctypes.data_as(vpt))
+        t_2p2 = time.perf_counter() - t0
+        res = {"kernel_sum": {"value": round(1.0 / t_pair, 4), "unit": "pairs/s", "seconds_per_pair": round(t_pair, 3),
+                              "reference_sums": ref.tolist(),
+                              "fp64_rel_err_vs_reference": float(np.max(np.abs(np.asarray(ours64) - ref) / np.abs(ref))),
+                              "headline_fp32_rel_err_vs_reference":
+                                  float(np.max(np.abs(np.asarray(ours32) - ref)) / np.max(np.abs(ref)))},
+               "kernel_memory_reserved_bytes": int(nb.value),
+               "what": "the reference's Contractor::kernel_sum and Contractor::pieces_2p2 driving its own "
+                       "kernels, built for sm_103a (oracle/ref_gpu), stand-in QED weight on the device; "
+                       "one pair of the first timed step (wall time of the blocking call)"}
+        if rc == 0:
+            ours = c.pieces_2p2(d_y, gsw, targets, xu, hg.FP64)
+            a = np.asarray(ours.p234).reshape(-1, 5, 64)
+            b = p234.reshape(-1, 5, 64)
+            err = max(float(np.abs(a[t, g] - b[t, g]).max() / max(np.abs(b[t, g]).max(), 1e-300))
+                      for t in range(b.shape[0]) for g in range(5))
+            res["pieces_2p2"] = {"value": round(t_2p2 * 1e3, 1), "unit": "ms per source",
+                                 "targets": N_TARGETS_2P2, "fp64_max_row_rel_err_vs_reference": err}
+        else:
+            res["pieces_2p2"] = {"unavailable": lib.refgpu_last_error().decode()}
+        return res
+    finally:
+        lib.refgpu_destroy(h)
 
 
 N_TARGETS_2P2 = 16  # the README's 2+2 timing is quoted per 16 targets

@@ -4,15 +4,21 @@
     python -m hlbl_gb300.build --lib    # library only
 
 The library is built in-tree under hlbl_gb300/_build/ (one nvcc process per
-translation unit, in parallel, then one link). The oracle (test
-infrastructure) goes to oracle/_build/. Where the reference sources are
-mounted, the host-emulation build of them (oracle/ref_host) is made too.
+translation unit, in parallel, then one link); a stamp beside it records the
+host architecture and compiler it was built for, and a library built for
+another is rebuilt. The oracle (test infrastructure) goes to oracle/_build/.
+Where the reference sources are found (HLBL_REFERENCE_DIR, else a `reference`
+directory beside the repository), the host-emulation build of them
+(oracle/ref_host) is made and the files of their GPU build are staged
+(oracle/ref_gpu); wherever a staged copy exists, the GPU build of the
+reference's kernels (oracle/_ref/gpu) is made too, alongside the library.
 """
 from __future__ import annotations
 
 import concurrent.futures as cf
 import glob
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -24,7 +30,9 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libhlbl_gb300.so")
 ORACLE_SRC = os.path.join(ROOT, "oracle", "hlbl_oracle.c")
 ORACLE_LIB = os.path.join(ROOT, "oracle", "_build", "libhlbl_oracle.so")
-REF_DIR = os.environ.get("HLBL_REFERENCE_DIR", "/root/reference")
+REF_DIR = os.environ.get("HLBL_REFERENCE_DIR", os.path.join(os.path.dirname(ROOT), "reference"))
+REF_GPU_SRC = os.path.join(ROOT, "oracle", "_ref", "gpu", "src")
+REF_GPU_LIB = os.path.join(ROOT, "oracle", "_ref", "gpu", platform.machine(), "libhlbl_ref_gpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
@@ -52,12 +60,26 @@ def _newer(target: str, deps) -> bool:
     return all(os.path.getmtime(d) <= t for d in deps)
 
 
+def _stamp() -> str:
+    """What the library was built for: host architecture, compiler, flags."""
+    r = subprocess.run([_nvcc(), "--version"], capture_output=True, text=True)
+    ver = r.stdout.strip().splitlines()[-1] if r.stdout.strip() else "?"
+    return "\n".join([platform.machine(), ver, " ".join(ARCH + NVCC_FLAGS)]) + "\n"
+
+
 def build_library(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     headers = sorted(glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))
                      + glob.glob(os.path.join(ROOT, "include", "*.h")))
-    if not force and _newer(LIB, sources + headers):
+    stamp_path = LIB + ".stamp"
+    stamp = _stamp()
+    try:
+        with open(stamp_path) as fh:
+            same = fh.read() == stamp
+    except OSError:
+        same = False
+    if not force and same and _newer(LIB, sources + headers):
         return LIB
     nvcc = _nvcc()
     objs = []
@@ -71,6 +93,8 @@ def build_library(force: bool = False) -> str:
     tmp = LIB + ".tmp"
     _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs)
     os.replace(tmp, LIB)
+    with open(stamp_path, "w") as fh:
+        fh.write(stamp)
     return LIB
 
 
@@ -88,11 +112,26 @@ def build_oracle(force: bool = False) -> str:
 
 
 def build_reference_emulation() -> str | None:
-    """The reference's own sources as a host emulation (only where mounted)."""
+    """The reference's own sources as a host emulation, and the staged copy of
+    the files of their GPU build (only where the sources are found)."""
     if not os.path.isdir(os.path.join(REF_DIR, "kernels")):
         return None
     _run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref_host"), "REF=" + REF_DIR])
+    _run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref_gpu"), "stage", "REF=" + REF_DIR])
     return os.path.join(ROOT, "oracle", "_ref", "libhlbl_ref_host.so")
+
+
+def build_reference_gpu() -> str | None:
+    """The reference's own kernels built for sm_103a from the staged copy
+    (the GPU baseline; None where no copy is staged or the build fails)."""
+    if not os.path.isdir(REF_GPU_SRC):
+        return None
+    r = subprocess.run(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle", "ref_gpu")],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        print("reference GPU build failed:\n" + r.stdout[-2000:] + r.stderr[-2000:], file=sys.stderr)
+        return None
+    return REF_GPU_LIB
 
 
 def main(argv=None) -> int:
@@ -102,6 +141,9 @@ def main(argv=None) -> int:
     if "--lib" not in argv:
         print(build_oracle(force))
         r = build_reference_emulation()
+        if r:
+            print(r)
+        r = build_reference_gpu()
         if r:
             print(r)
     return 0

@@ -174,3 +174,69 @@ def pair_rel_err(a, b) -> float:
 def rel_err(a, b) -> float:
     a, b = np.asarray(a, dtype=float), np.asarray(b, dtype=float)
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+
+
+# ---- the reference's own kernels built for the GPU (oracle/ref_gpu) ---------
+_ref_gpu = None
+
+
+def ref_gpu_lib():
+    """The GPU build of the reference's Contractor and kernels, or None where
+    no staged copy of its sources was built (a machine without the reference
+    checkout and without the copy)."""
+    global _ref_gpu
+    if _ref_gpu is None:
+        import platform
+
+        path = os.path.join(ROOT, "oracle", "_ref", "gpu", platform.machine(), "libhlbl_ref_gpu.so")
+        if not os.path.exists(path):
+            return None
+        lib = C.CDLL(path)
+        vpt = C.c_void_p
+        lib.refgpu_last_error.restype = C.c_char_p
+        lib.refgpu_create.argtypes = [C.POINTER(vpt), I4, C.c_int, C.c_ulonglong]
+        lib.refgpu_destroy.argtypes = [vpt]
+        lib.refgpu_kernel_sum.argtypes = [vpt, vpt, vpt, I4, I4, C.c_double, vpt]
+        lib.refgpu_pieces_2p2.argtypes = [vpt, vpt, I4, vpt, C.c_int, C.c_double, vpt, vpt]
+        lib.refgpu_reserve_kernel_memory.argtypes = [vpt, C.c_int, C.POINTER(C.c_size_t)]
+        _ref_gpu = lib
+    return _ref_gpu
+
+
+class RefGpu:
+    """The reference's Contractor on the GPU (one rank, whole lattice), with
+    the stand-in weight or (dense) the dense test weight."""
+
+    def __init__(self, lattice, dense=False, seed=DENSE_SEED):
+        self.lib = ref_gpu_lib()
+        self.h = C.c_void_p()
+        self._check(self.lib.refgpu_create(C.byref(self.h), i4(lattice), int(bool(dense)), seed))
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError(self.lib.refgpu_last_error().decode())
+
+    def kernel_sum(self, d_src, d_y, gsx, yv, xunit):
+        out = (C.c_double * 2)()
+        self._check(self.lib.refgpu_kernel_sum(self.h, C.c_void_p(d_src.data_ptr()),
+                                               C.c_void_p(d_y.data_ptr()), i4(gsx), i4(yv),
+                                               C.c_double(xunit), out))
+        return out[0], out[1]
+
+    def pieces_2p2(self, d_fwd, gsw, targets, xunit, lmax):
+        tg = np.ascontiguousarray(np.asarray(targets, dtype=np.int32).reshape(-1, 4))
+        p1, p234 = np.zeros(64 * lmax), np.zeros(len(tg) * 5 * 64)
+        self._check(self.lib.refgpu_pieces_2p2(self.h, C.c_void_p(d_fwd.data_ptr()), i4(gsw), vp(tg),
+                                               len(tg), C.c_double(xunit), vp(p1), vp(p234)))
+        return p1, p234.reshape(len(tg), 5, 64)
+
+    def close(self):
+        if self.h:
+            self.lib.refgpu_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
