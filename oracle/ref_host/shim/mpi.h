@@ -40,3 +40,5 @@ inline int MPI_Iallreduce(const void* s, void* r, int n, MPI_Datatype t, MPI_Op 
 inline int MPI_Waitall(int, MPI_Request*, void*) { return 0; }
 inline int MPI_Abort(MPI_Comm, int e) { std::exit(e); }
 inline double MPI_Wtime() { return 0.0; }
+inline int MPI_Init(int*, char***) { return 0; }
+inline int MPI_Finalize() { return 0; }
