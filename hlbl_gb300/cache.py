@@ -2,12 +2,16 @@
 (include/hlbl/propagator_cache.hpp, src/propagator_cache.cpp of the
 reference), same states, same errors, same peak accounting.
 
-  device  blocks on the GPU, read in place.
-  host    blocks in pinned host memory; a contraction gets its block through
-          one of two device staging slots. Unlike the reference's
-          synchronous cudaMemcpy (propagator_cache.cpp:63-66), the copy is
-          issued on the contractor's side stream (hlbl_stage_async), so the
-          next source's block streams in while the current one computes.
+  device    blocks on the GPU, read in place.
+  host      blocks in pinned host memory; a contraction gets its block through
+            one of two device staging slots. Unlike the reference's
+            synchronous cudaMemcpy (propagator_cache.cpp:63-66), the copy is
+            issued on the contractor's side stream (hlbl_stage_async), so the
+            next source's block streams in while the current one computes.
+  device32  the FP32 tile copy of each block on the GPU (half the bytes):
+            the solve fills one FP64 scratch block, which is converted into
+            the entry's copy as it is stored (hlbl_f32_tile_copy); the
+            FP32-copy contraction path (kernel_sums_batched_f32) reads them.
 
 Buffers come from an allocator object, so the bookkeeping is testable
 without a GPU: TorchBuffers (the product) or any object with the same three
@@ -18,7 +22,7 @@ from __future__ import annotations
 from typing import Dict, Optional, Tuple
 
 Vec4 = Tuple[int, int, int, int]
-DEVICE, HOST = "device", "host"
+DEVICE, HOST, DEVICE32 = "device", "host", "device32"
 
 
 class TorchBuffers:
@@ -43,13 +47,19 @@ class TorchBuffers:
         self.c.check()  # the solve that filled src_dev ran on the contractor's stream
         dst_host.copy_(src_dev)
 
+    def device32(self):
+        return self.torch.empty(self.c.f32_block_length, dtype=self.torch.float32, device="cuda")
+
+    def convert(self, dst32, src_dev):
+        self.c.f32_tile_copy(src_dev, dst32)  # on the contractor's stream, after the solve
+
 
 class PropagatorCache:
     """Mirror of hlbl::PropagatorCache (propagator_cache.hpp:24-75)."""
 
     def __init__(self, residency: str, block_len: int, buffers, pending: Optional[Dict] = None):
-        if residency not in (DEVICE, HOST):
-            raise ValueError("residency is 'device' or 'host'")
+        if residency not in (DEVICE, HOST, DEVICE32):
+            raise ValueError("residency is 'device', 'host' or 'device32'")
         self.residency = residency
         self.block_len = block_len
         self.buf = buffers
@@ -85,6 +95,10 @@ class PropagatorCache:
             h = self.pool.pop() if self.pool else self.buf.pinned(self.block_len)
             self.buf.store(h, self.scratch)
             self.entries[position] = h
+        elif self.residency == DEVICE32:
+            h = self.pool.pop() if self.pool else self.buf.device32()
+            self.buf.convert(h, self.scratch)
+            self.entries[position] = h
         self.peak = max(self.peak, len(self.entries))
         if self.pending.get(position, 0) == 0:
             self._evict(position)
@@ -94,7 +108,7 @@ class PropagatorCache:
         unless it is there already (propagator_cache.cpp:52-68)."""
         if position not in self.entries:
             raise RuntimeError("PropagatorCache: position is not cached")
-        if self.residency == DEVICE:
+        if self.residency in (DEVICE, DEVICE32):
             return self.entries[position]
         if slot not in (0, 1):
             raise RuntimeError("PropagatorCache: bad slot")
@@ -121,7 +135,7 @@ class PropagatorCache:
     def _evict(self, position: Vec4) -> None:
         """propagator_cache.cpp:80-91"""
         e = self.entries.pop(position, None)
-        if e is not None and self.residency == HOST:
+        if e is not None and self.residency in (HOST, DEVICE32):
             self.pool.append(e)
         for i in (0, 1):
             if self.staged[i] == position:

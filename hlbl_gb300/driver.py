@@ -4,7 +4,9 @@ their last pair. Two pair loops:
 
   per_pair  Contractor.kernel_sum once per pair, as driver.cpp:104-134 does;
   batched   one kernel_sums_batched per new source (all pairs it closes share
-            its block), optionally recorded as one CUDA graph per window.
+            its block), optionally recorded as one CUDA graph per window;
+            with the device32 cache (FP32 tile copies of the blocks, made as
+            each block is stored) one kernel_sums_batched_f32 per new source.
 
 With `sources_2p2` ({global site: [targets]}), the first solve of each of
 those sites computes its 2+2 pieces from the freshly solved block, before the
@@ -110,8 +112,11 @@ def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cach
             stats.pieces_2p2 += 1
             stats.targets_2p2 += len(targets)
         cache.end_insert(position)
-    if batched and cache.residency != "device":
-        raise ValueError("the batched loop needs the device cache (every partner resident)")
+    if batched and cache.residency not in ("device", "device32"):
+        raise ValueError("the batched loop needs a device cache (every partner resident)")
+    if cache.residency == "device32" and not batched:
+        raise ValueError("the device32 cache (FP32 copies) feeds the batched FP32-copy loop only")
+    f32 = cache.residency == "device32"
     for st in steps:
         window_rows = []
         if not batched:
@@ -154,7 +159,10 @@ def run_chain(steps, lattice, xunit: float, provider: Callable, contractor, cach
             if graphs:
                 contractor.graph_begin()
             for d_y, xs, gxs, yvs, _, buf, _ in calls:
-                contractor.kernel_sums_batched(d_y, xs, gxs, yvs, xunit, buf, precision)
+                if f32:
+                    contractor.kernel_sums_batched_f32(d_y, xs, gxs, yvs, xunit, buf)
+                else:
+                    contractor.kernel_sums_batched(d_y, xs, gxs, yvs, xunit, buf, precision)
             if graphs:
                 g = contractor.graph_end()
                 g.launch()

@@ -85,7 +85,10 @@ int hlbl_kernel_sum_async(hlbl_ctx* ctx, const double* d_fwd_src, const double* 
  * solved source closes): pair i is (x = gsx[i], y = gsx[i] + yv[i]) with
  * the partner block srcs[i] (host array of device pointers); both flavours
  * to d_out[2*i..2*i+1] (device). Pairs run in batched launches of up to 16
- * (hlbl_ctx_set_batch_group) that read y once for all of them.
+ * (hlbl_ctx_set_batch_group): the pairs of a launch walk y's tiles in step,
+ * so L2 can serve y to the partners after the first; each pair's CTAs still
+ * read y themselves, and as the kernels are bound by arithmetic rather than
+ * HBM, the autotuner usually keeps one pair per launch.
  * Asynchronous on the context's stream; capturable into a CUDA graph.
  * The per-source batching of the driver's pair loop (src/driver.cpp:104-134),
  * which calls Contractor::kernel_sum once per pair. */

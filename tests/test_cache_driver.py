@@ -26,6 +26,12 @@ class NumpyBuffers:
     def store(self, dst, src):
         dst[:] = src
 
+    def device32(self):
+        return np.zeros(4, dtype=np.float32)
+
+    def convert(self, dst32, src):
+        dst32[:] = src[:4]
+
 
 class Recorder:
     """Stands in for the Contractor: returns a value the test can predict."""
@@ -60,6 +66,63 @@ def test_driver_loop_matches_schedule_simulation(residency):
     if residency == "host":
         # slot 0 stays staged across a source's partners (propagator_cache.cpp:63-66)
         assert buf.staged < 2 * n_pairs
+
+
+class BatchRecorder:
+    """Stands in for the Contractor's batched calls (FP64 blocks or FP32
+    copies), writing a value the test can predict into the output rows."""
+
+    def __init__(self):
+        self.calls = {"f64": 0, "f32": 0}
+
+    def _fill(self, d_y, xs, gxs, yvs, out):
+        for i, (x, g, v) in enumerate(zip(xs, gxs, yvs)):
+            out[i] = (float(x[0] + 10 * d_y[0]), float(sum(g) + sum(v)))
+
+    def kernel_sums_batched(self, d_y, xs, gxs, yvs, xunit, out, precision):
+        self.calls["f64"] += 1
+        self._fill(d_y, xs, gxs, yvs, out)
+
+    def kernel_sums_batched_f32(self, d_y32, xs, gxs, yvs, xunit, out):
+        assert d_y32.dtype == np.float32 and all(x.dtype == np.float32 for x in xs)
+        self.calls["f32"] += 1
+        self._fill(d_y32, xs, gxs, yvs, out)
+
+    def check(self):
+        pass
+
+
+class Rows(np.ndarray):
+    def cpu(self):
+        return self
+
+
+@pytest.mark.parametrize("residency", ["device", "device32"])
+def test_batched_loop_on_fp64_blocks_and_fp32_copies(residency):
+    """The batched loop over the device cache (FP64 blocks) and the device32
+    cache (FP32 copies converted as each block is stored): the same pairs and
+    values as the per-pair loop, one batched call per source with partners,
+    and the copies' buffers reused after eviction."""
+    lat = (6, 6, 6, 6)
+    steps = schedule.build_schedule((1, 1, 1, 1), 1, 2)
+    n_prop, n_pairs, _ = schedule.simulate(steps)
+    ref, _ = run_chain(steps, lat, 0.1, provider, Recorder(), PropagatorCache("device", 4, NumpyBuffers()))
+    rec = BatchRecorder()
+    cache = PropagatorCache(residency, 4, NumpyBuffers())
+    res, st = run_chain(steps, lat, 0.1, provider, rec, cache, batched=True,
+                        out_factory=lambda n: np.zeros((n, 2)).view(Rows))
+    assert st.pairs == n_pairs == len(res) and st.positions_solved == n_prop
+    assert sorted((r.x, r.y) for r in res) == sorted((r.x, r.y) for r in ref)
+    want = {(r.x, r.y): r.kernel_sum[0] for r in ref}
+    assert all(r.kernel_sum[0] == want[(r.x, r.y)] for r in res)
+    n_src = sum(1 for stp in steps for src in stp.sources if src.partners)
+    assert rec.calls == ({"f64": 0, "f32": n_src} if residency == "device32" else {"f64": n_src, "f32": 0})
+    if residency == "device32":
+        # one copy buffer per entry alive at the peak (the batched loop solves a
+        # whole window first), reused after eviction
+        assert cache.scratch is not None and len(cache.pool) + cache.size() == st.cache_peak
+    with pytest.raises(ValueError):
+        run_chain(steps, lat, 0.1, provider, Recorder(), PropagatorCache("device32", 4, NumpyBuffers()))
 
 
 def test_driver_2p2_at_first_solves():

@@ -131,3 +131,39 @@ def test_run_chains_equals_independent_chains(tmp_path):
         assert np.array_equal(f["2p2/P234"].reshape(-1, 5, 64), np.asarray(out22[0].p234).reshape(-1, 5, 64))
         rows = open(tmp_path / "timing.csv").read().splitlines()[1:]
         assert sum(r.startswith("kernel_sum,") for r in rows) == st.pairs
+
+
+def test_driver_fp32_copies_chain_total():
+    """The batched loop on the device32 cache (FP32 tile copies made as each
+    block is stored, kernel_sums_batched_f32, a CUDA graph per window) over a
+    whole chain (stride 2, two steps) of a 16^4 lattice with Gaussian fields:
+    every pair within 1e-4 of the FP64 per-pair loop at the pair's scale, and
+    each flavour's chain total within 1e-6."""
+    import hlbl_gb300 as hg
+    from hlbl_gb300 import schedule
+    from hlbl_gb300.cache import PropagatorCache, TorchBuffers
+    from hlbl_gb300.driver import run_chain
+
+    lat = (16, 16, 16, 16)
+    xu = hg.xunit(105.658, 0.1)
+    steps = schedule.build_schedule((1, -1, 1, -1), 2, 2)
+    with hg.Contractor(lat) as c:
+        def provider(site, dest):
+            c.fill_gaussian_block(dest, hg.Contractor.source_seed(11, site))
+
+        f64, _ = run_chain(steps, lat, xu, provider, c, PropagatorCache("device", c.block_length, TorchBuffers(c)),
+                           precision=hg.FP64)
+        f32, st = run_chain(steps, lat, xu, provider, c,
+                            PropagatorCache("device32", c.block_length, TorchBuffers(c)), batched=True,
+                            graphs=True,
+                            out_factory=lambda n: torch.zeros((n, 2), dtype=torch.float64, device="cuda"))
+    ref = {(r.x, r.y): r.kernel_sum for r in f64}
+    assert len(f32) == len(f64) == st.pairs
+    worst = max(S.pair_rel_err(r.kernel_sum, ref[(r.x, r.y)]) for r in f32)
+    tot32 = np.sum([r.kernel_sum for r in f32], axis=0)
+    tot64 = np.sum([r.kernel_sum for r in f64], axis=0)
+    chain = float(np.max(np.abs(tot32 - tot64) / np.abs(tot64)))
+    print(f"CHAIN pairs {len(f32)}: worst pair {worst:.3e}, chain total {chain:.3e}, "
+          f"totals {tot64.tolist()}, max |pair| {max(max(abs(v) for v in r) for r in ref.values()):.3e}")
+    assert worst <= 1e-4
+    assert chain <= 1e-6, (tot32, tot64)
