@@ -32,6 +32,8 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "contract_kernels.cuh"
 
 namespace hg {
@@ -74,6 +76,9 @@ struct QedStandIn {
 
 struct QedDense {
   static constexpr int kState = HLBL_QED_DENSE_NB;
+  // every entry is linear in the state: entry(st, i) = sum_b table[b][i] st[b]
+  // (qed_coef.cu's coefficient stage has a kernel for such providers)
+  static constexpr bool kLinear = true;
   const double* t64;  // [13][384], device
   const float* t32;   // the same rounded to FP32
   template <typename T>
@@ -141,6 +146,11 @@ decltype(auto) with_provider(const QedSel& q, F&& f) {
   if (q.kind == kQedDenseKerv) return f(QedDenseKerv{DenseKervFn{q.t64}});
   return f(QedStandIn{q.qp});
 }
+
+template <class P, class = void>
+struct IsLinear : std::false_type {};
+template <class P>
+struct IsLinear<P, std::void_t<decltype(P::kLinear)>> : std::bool_constant<P::kLinear> {};
 
 // One coefficient of a site from its three evaluations' states.
 template <class P, typename T>

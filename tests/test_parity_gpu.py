@@ -207,3 +207,29 @@ def test_errors_are_reported(hg):
     with pytest.raises(hg.HlblError):
         hg.Contractor((4, 4, 4, 4), (4, 4, 4, 3), (0, 0, 0, 1))  # 2*3 > 4
     assert hg.Contractor(lat).reserve_kernel_memory() >= 0
+
+
+def test_reserve_kernel_memory_reserves_once():
+    """Contractor::reserve_kernel_memory (contract.cpp:158-197) warm-launches
+    the kernels so that whatever the first launches take is taken before
+    free memory is measured. The library's kernels keep no per-thread stack
+    (the reference's 4-point kernel reserves ~27 KB per thread slot, 3.7 GB
+    on this GPU), so: the first call takes well under the reference's
+    figure, a second call takes nothing more, and contractions of every
+    precision afterwards leave free device memory where it was."""
+    import hlbl_gb300 as hg
+
+    lat = (2, 2, 2, 2)
+    mib = 1 << 20
+    with hg.Contractor(lat) as c:
+        first = c.reserve_kernel_memory()
+        second = c.reserve_kernel_memory()
+        assert first < 512 * mib, first
+        assert second <= 2 * mib, second  # the allocation granularity at most
+        d = dev(S.random_block(lat, 3))
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        for prec in (hg.FP64, hg.FP32):
+            c.kernel_sum(d, d, (0, 0, 0, 0), (1, 1, 1, 1), 1.0, prec)
+        torch.cuda.synchronize()
+        assert abs(torch.cuda.mem_get_info()[0] - free0) <= 2 * mib
