@@ -409,6 +409,8 @@ QedSel qed_sel(const hlbl_ctx* c) {
   QedSel q;
   q.kind = c->qed_kind;
   q.qp = c->qp;
+  q.qf = c->qf;
+  q.r64 = c->qed_fp32 ? c->qed_r64 : 1e300;  // the FP32 path's weight setting (hlbl_ctx_set_qed_fp32)
   q.t64 = c->d_dense64;
   q.t32 = c->d_dense32;
   return q;

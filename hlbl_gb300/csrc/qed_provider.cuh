@@ -55,11 +55,22 @@ __host__ __device__ constexpr int kerv_index(int k, int mu, int nu, int lam) {
 struct QedStandIn {
   static constexpr int kState = 14;
   hlbl_qed_params qp;
+  QedF32 qf;      // its FP32 quadrature tables (qed_f32.cuh)
+  double r64;     // FP32 states: the FP64 weights where min(|a|, |b|) < r64
   template <typename T>
   __device__ __forceinline__ void prepare(const double a[4], const double b[4], T* st) const {
     double X, c, Y, w[HLBL_QED_NW];
     hlbl_qed_invariants(a, b, &X, &c, &Y);
-    hlbl_qed_weights(&qp, X, c, Y, w);
+    if (sizeof(T) == 4 && fmin(X, Y) >= r64) {
+      // the FP32 path's weight, as the closed-form FP32 path evaluates it
+      float wf[HLBL_QED_NW];
+      if (qf.geometric) weights_f32<true, false>(qf, (float)X, (float)c, (float)Y, wf);
+      else weights_f32<false, false>(qf, (float)X, (float)c, (float)Y, wf);
+#pragma unroll
+      for (int j = 0; j < HLBL_QED_NW; ++j) w[j] = wf[j];
+    } else {
+      hlbl_qed_weights(&qp, X, c, Y, w);
+    }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       st[r] = (T)a[r];
@@ -135,6 +146,8 @@ using QedDenseKerv = QedKerv<DenseKervFn>;
 struct QedSel {
   int kind = kQedStandInClosed;
   hlbl_qed_params qp{};
+  QedF32 qf{};
+  double r64 = 0.0;
   const double* t64 = nullptr;
   const float* t32 = nullptr;
 };
@@ -144,7 +157,7 @@ template <class F>
 decltype(auto) with_provider(const QedSel& q, F&& f) {
   if (q.kind == kQedDense) return f(QedDense{q.t64, q.t32});
   if (q.kind == kQedDenseKerv) return f(QedDenseKerv{DenseKervFn{q.t64}});
-  return f(QedStandIn{q.qp});
+  return f(QedStandIn{q.qp, q.qf, q.r64});
 }
 
 template <class P, class = void>
