@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-chains16", action="store_true", help="skip the 16-chain driver run")
+    ap.add_argument("--config5", action="store_true",
+                    help="the 48^3x96 host-cache line alone (about 75 GB of pinned host memory)")
+    ap.add_argument("--c5-partners", type=int, default=3)
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="skip the baseline leg of the reference's own kernels on the GPU")
     ap.add_argument("--no-autotune", action="store_true",
@@ -237,6 +240,8 @@ def main():
     from hlbl_gb300.contract import measure_fma_peak
 
     torch.cuda.set_device(local_rank)
+    if args.config5:
+        return run_config5(args, hg, torch, rank)
     if args.only_2p2:
         return run_2p2_only(args, hg, torch, rank)
     dist = None
@@ -936,6 +941,138 @@ def bench_2p2(c, hg, torch, stream, fwd, x32, gsw, xu, reps):
             "gpu_launches_per_source": 3 + 5 * ((N_TARGETS_2P2 + 31) // 32),
             "reference_readme": "compute_2p2_gpu 4.6 s per 16 targets, one GH200, 262,144 sites, "
                                 "real KQED (not comparable weight)"}
+
+
+def run_config5(args, hg, torch, rank):
+    """The 48^3 x 96 configuration (V = 10,616,832; a 49 GB FP64 block, a
+    24.5 GB FP32 tile copy) with a host-resident cache: stride 4,
+    h = (-1,+1,+1,+1), K = 8, one source of window 1 and `c5_partners` of its
+    partners. The partners' blocks are solved (device fixtures), converted to
+    FP32 tile copies and stored in pinned host memory; in the timed loop each
+    partner's copy streams into one of two device slots on a copy stream while
+    the previous pair computes (one FP32-copy kernel-sum call per pair), so
+    a pair costs max(copy, compute). Reported: pairs/s overlapped and with
+    copy and compute in sequence, the host-to-device GB/s, and the first
+    pair's error against the FP64 path. The GPU machine's host has 199 GB, so
+    the reference's cache of FP64 blocks (16 live 49 GB blocks) cannot exist
+    there; the host cache holds FP32 copies."""
+    from hlbl_gb300 import schedule
+
+    if rank != 0:
+        return 0
+    lat = (96, 48, 48, 48)
+    h, stride, K = (-1, 1, 1, 1), 4, 8
+    xu = hg.xunit(MUON_MEV, SPACING_FM)
+    st = schedule.build_schedule(h, stride, K)
+    src = next(s_ for s_ in st[1].sources if len(s_.partners) >= args.c5_partners)
+    p = src.position
+    qs = list(src.partners)[:args.c5_partners]
+    c = hg.Contractor(lat)
+    stream = torch.cuda.Stream()
+    copy_stream = torch.cuda.Stream()
+    c.set_stream(stream)
+    n32 = c.f32_block_length
+    site = lambda q: schedule.mod_pos(q, lat)  # noqa: E731
+    seed = lambda q: hg.Contractor.source_seed(RUN_SEED, site(q))  # noqa: E731
+    t0 = time.perf_counter()
+    scratch = torch.empty(c.block_length, dtype=torch.float64, device="cuda")
+    y32 = torch.empty(n32, dtype=torch.float32, device="cuda")
+    slots = [torch.empty(n32, dtype=torch.float32, device="cuda") for _ in range(2)]
+    host = []
+    with torch.cuda.stream(stream):
+        for q in qs:
+            c.fill_gaussian_block(scratch, seed(q))
+            c.f32_tile_copy(scratch, slots[0])
+            hq = torch.empty(n32, dtype=torch.float32, pin_memory=True)
+            hq.copy_(slots[0])
+            host.append(hq)
+        c.fill_gaussian_block(scratch, seed(p))
+        c.f32_tile_copy(scratch, y32)
+    stream.synchronize()
+    del scratch
+    t_setup = time.perf_counter() - t0
+    out = torch.zeros((len(qs), 2), dtype=torch.float64, device="cuda")
+    gsx = [site(q) for q in qs]
+    yvs = [schedule.site_map_diff(p, q, lat) for q in qs]
+
+    def one_pass():
+        """Copy i goes to slot i % 2 on the copy stream once pair i - 2 (the
+        slot's last reader) is done; pair i computes once copy i landed."""
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        staged = [torch.cuda.Event() for _ in qs]
+        done = [torch.cuda.Event() for _ in qs]
+        copy_ev = []
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        copy_stream.wait_stream(stream)
+
+        def copy(i):
+            if i >= 2:
+                copy_stream.wait_event(done[i - 2])
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(copy_stream):
+                e0.record(copy_stream)
+                slots[i % 2].copy_(host[i], non_blocking=True)
+                e1.record(copy_stream)
+                staged[i].record(copy_stream)
+            copy_ev.append((e0, e1))
+
+        copy(0)
+        for i in range(len(qs)):
+            if i + 1 < len(qs):
+                copy(i + 1)
+            stream.wait_event(staged[i])
+            c.kernel_sums_batched_f32(y32, [slots[i % 2]], [gsx[i]], [yvs[i]], xu, out[i:i + 1])
+            done[i].record(stream)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        gbs = [n32 * 4 / (a.elapsed_time(b) * 1e-3) / 1e9 for a, b in copy_ev]
+        return ev0.elapsed_time(ev1), gbs
+
+    one_pass()  # untimed: first launches at this size
+    ms_ov, gbs_ov = one_pass()
+    res32 = out.cpu().numpy().copy()
+    # copies and computes in sequence: the reference's order (it copies
+    # synchronously before each pair, propagator_cache.cpp:52-68)
+    c.check()
+    ms_seq, gbs_seq = [], []
+    for i in range(len(qs)):
+        torch.cuda.synchronize()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            slots[0].copy_(host[i], non_blocking=True)
+            e1.record(stream)
+            c.kernel_sums_batched_f32(y32, [slots[0]], [gsx[i]], [yvs[i]], xu, out[i:i + 1])
+            e2.record(stream)
+        e2.synchronize()
+        ms_seq.append(e0.elapsed_time(e2))
+        gbs_seq.append(n32 * 4 / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+    del slots, y32
+    torch.cuda.synchronize()
+    # the first pair by the FP64 path on the FP64 blocks
+    x64 = torch.empty(c.block_length, dtype=torch.float64, device="cuda")
+    y64 = torch.empty(c.block_length, dtype=torch.float64, device="cuda")
+    with torch.cuda.stream(stream):
+        c.fill_gaussian_block(x64, seed(qs[0]))
+        c.fill_gaussian_block(y64, seed(p))
+    stream.synchronize()
+    t0 = time.perf_counter()
+    f64 = c.kernel_sum(x64, y64, gsx[0], yvs[0], xu, hg.FP64)
+    t64 = time.perf_counter() - t0
+    err = max(abs(res32[0][f] - f64[f]) for f in (0, 1)) / max(abs(f64[0]), abs(f64[1]))
+    r = {"metric": "pairs/s at 48^3x96 with a host-resident cache (FP32 tile copies staged per pair)",
+         "value": round(len(qs) / (ms_ov * 1e-3), 3), "unit": "pairs/s", "pairs": len(qs),
+         "lattice": list(lat), "h": list(h), "stride": stride, "K": K,
+         "source": list(site(p)), "partners": [list(site(q)) for q in qs],
+         "sequential_pairs_per_s": round(len(qs) / (sum(ms_seq) * 1e-3), 3),
+         "h2d_gbs_overlapped": [round(g, 1) for g in gbs_ov], "h2d_gbs_sequential": [round(g, 1) for g in gbs_seq],
+         "bytes_staged_per_pair": n32 * 4, "setup_seconds": round(t_setup, 1),
+         "fp64_seconds_per_pair": round(t64, 2), "fp32_rel_err_vs_fp64_first_pair": err,
+         "path": "FP32 tile copies in pinned host memory, two device slots, copy stream overlapped with the "
+                 "FP32-copy kernel sums (tensor-core pass 2)"}
+    print(json.dumps(r), flush=True)
+    return 0
 
 
 def run_2p2_only(args, hg, torch, rank):
