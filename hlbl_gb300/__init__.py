@@ -11,10 +11,10 @@ from importlib import import_module
 
 _LAZY = {"Contractor": "contract", "FP64": "contract", "FP32": "contract", "xunit": "contract",
          "HlblError": "_lib", "QED_STANDIN": "contract", "QED_STANDIN_GENERIC": "contract",
-         "QED_DENSE": "contract", "QED_DENSE_KERV": "contract"}
+         "QED_DENSE": "contract", "QED_DENSE_KERV": "contract", "QED_KQED": "contract"}
 
 __all__ = ["Contractor", "FP64", "FP32", "xunit", "HlblError", "schedule", "QED_STANDIN",
-           "QED_STANDIN_GENERIC", "QED_DENSE", "QED_DENSE_KERV"]
+           "QED_STANDIN_GENERIC", "QED_DENSE", "QED_DENSE_KERV", "QED_KQED"]
 
 
 def __getattr__(name):

@@ -1,14 +1,17 @@
 """ctypes binding of libhlbl_gb300.so (the C ABI of include/hlbl_gb300.h).
 
 The library is the product: there is no fallback. If it is missing this
-module raises at import, naming the build command.
+module raises at import, naming the build command. HLBL_GB300_LIB selects
+another build of it (for example one linked with a KQED).
 """
 from __future__ import annotations
 
 import ctypes as C
 import os
 
-from .build import LIB
+from .build import LIB as _DEFAULT_LIB
+
+LIB = os.environ.get("HLBL_GB300_LIB") or _DEFAULT_LIB
 
 I4 = C.c_int * 4
 

@@ -60,42 +60,62 @@ def _newer(target: str, deps) -> bool:
     return all(os.path.getmtime(d) <= t for d in deps)
 
 
-def _stamp() -> str:
+def _stamp(flags) -> str:
     """What the library was built for: host architecture, compiler, flags."""
     r = subprocess.run([_nvcc(), "--version"], capture_output=True, text=True)
     ver = r.stdout.strip().splitlines()[-1] if r.stdout.strip() else "?"
-    return "\n".join([platform.machine(), ver, " ".join(ARCH + NVCC_FLAGS)]) + "\n"
+    return "\n".join([platform.machine(), ver, " ".join(ARCH + flags)]) + "\n"
 
 
-def build_library(force: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def _kqed_flags(kqed_dir):
+    """A linked KQED: its header directory and static library (include/KQED.h,
+    lib/libKQED_cuda.a under kqed_dir); its device code needs relocatable
+    device code and a device link."""
+    inc, lib = os.path.join(kqed_dir, "include"), os.path.join(kqed_dir, "lib", "libKQED_cuda.a")
+    for p in (os.path.join(inc, "KQED.h"), lib):
+        if not os.path.exists(p):
+            raise RuntimeError(f"HLBL_KQED_DIR: {p} is missing")
+    return ["-DHLBL_WITH_KQED", "-rdc=true", "-I", inc], [lib], [inc, lib]
+
+
+def build_library(force: bool = False, kqed_dir: str | None = None, out: str | None = None) -> str:
+    """The library; with kqed_dir (default: the HLBL_KQED_DIR environment
+    variable) linked with that KQED, so that HLBL_QEDK_KQED weights with its
+    QED_Mkernel_L2. `out`: the library's path (default hlbl_gb300/_build)."""
+    kqed_dir = kqed_dir if kqed_dir is not None else os.environ.get("HLBL_KQED_DIR") or None
+    lib_path = out or LIB
+    build_dir = os.path.dirname(lib_path)
+    os.makedirs(build_dir, exist_ok=True)
+    extra, link_extra, deps_extra = _kqed_flags(kqed_dir) if kqed_dir else ([], [], [])
+    flags = NVCC_FLAGS + extra
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     headers = sorted(glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))
                      + glob.glob(os.path.join(ROOT, "include", "*.h")))
-    stamp_path = LIB + ".stamp"
-    stamp = _stamp()
+    deps = sources + headers + [d for d in deps_extra if os.path.isfile(d)]
+    stamp_path = lib_path + ".stamp"
+    stamp = _stamp(flags + link_extra)
     try:
         with open(stamp_path) as fh:
             same = fh.read() == stamp
     except OSError:
         same = False
-    if not force and same and _newer(LIB, sources + headers):
-        return LIB
+    if not force and same and _newer(lib_path, deps):
+        return lib_path
     nvcc = _nvcc()
     objs = []
     jobs = []
     for s in sources:
-        o = os.path.join(BUILD, os.path.basename(s)[:-3] + ".o")
+        o = os.path.join(build_dir, os.path.basename(s)[:-3] + ".o")
         objs.append(o)
-        jobs.append([nvcc] + ARCH + NVCC_FLAGS + ["-c", s, "-o", o])
+        jobs.append([nvcc] + ARCH + flags + ["-c", s, "-o", o])
     with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
         list(ex.map(_run, jobs))
-    tmp = LIB + ".tmp"
-    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs)
-    os.replace(tmp, LIB)
+    tmp = lib_path + ".tmp"
+    _run([nvcc] + ARCH + (["-rdc=true"] if kqed_dir else []) + ["-shared", "-o", tmp] + objs + link_extra)
+    os.replace(tmp, lib_path)
     with open(stamp_path, "w") as fh:
         fh.write(stamp)
-    return LIB
+    return lib_path
 
 
 def build_oracle(force: bool = False) -> str:

@@ -19,7 +19,7 @@ FP32 = 1  # per-site products in FP32, FP64 site and volume sums
 # QED kernels (hlbl_ctx_set_qed_kernel): the stand-in through its closed-form
 # paths, the stand-in through the generic paths, the dense test weight (no
 # index structure) entry by entry, and the same as a whole-tensor function
-QED_STANDIN, QED_STANDIN_GENERIC, QED_DENSE, QED_DENSE_KERV = 0, 1, 2, 3
+QED_STANDIN, QED_STANDIN_GENERIC, QED_DENSE, QED_DENSE_KERV, QED_KQED = 0, 1, 2, 3, 4
 HBARC_MEV_FM = 197.3269804  # include/hlbl/physics.hpp:9
 
 
@@ -327,7 +327,8 @@ class Contractor:
     # -- the QED weight ------------------------------------------------------
     def set_qed_kernel(self, kind: int, seed: int = 0) -> None:
         """The QED kernel pass 2 and the 2+2 pieces weight with (QED_STANDIN,
-        QED_STANDIN_GENERIC, QED_DENSE with its table seed, QED_DENSE_KERV)."""
+        QED_STANDIN_GENERIC, QED_DENSE with its table seed, QED_DENSE_KERV,
+        QED_KQED in a build linked with a KQED)."""
         check(lib.hlbl_ctx_set_qed_kernel(self._h, int(kind), C.c_uint64(seed)))
 
     def set_qed(self, surrogate=None, r0: float = -1.0) -> None:

@@ -253,6 +253,10 @@ struct hlbl_ctx {
   double* d_dense64 = nullptr;  // the dense test weight's table [13][384]
   float* d_dense32 = nullptr;
   void* d_coef = nullptr;       // generic path: coefficients of a pair group
+#ifdef HLBL_WITH_KQED
+  QED_kernel_temps kq{};        // a linked KQED's temps (initialise())
+  bool kq_ready = false;
+#endif
   size_t coef_cap = 0;          // bytes of d_coef
   int batch_group = 0;        // pairs per batched launch (0: kMaxBatch)
   int qed_mode = HLBL_QED_EXACT;
@@ -413,6 +417,9 @@ QedSel qed_sel(const hlbl_ctx* c) {
   q.r64 = c->qed_fp32 ? c->qed_r64 : 1e300;  // the FP32 path's weight setting (hlbl_ctx_set_qed_fp32)
   q.t64 = c->d_dense64;
   q.t32 = c->d_dense32;
+#ifdef HLBL_WITH_KQED
+  q.kq = c->kq;
+#endif
   return q;
 }
 
@@ -1172,6 +1179,16 @@ void hlbl_graph_destroy(hlbl_graph* g) {
 int hlbl_ctx_set_qed_kernel(hlbl_ctx* c, int kind, uint64_t seed) {
   if (!c) return fail(HLBL_EINVAL, "hlbl_ctx_set_qed_kernel: null context");
   if (kind < 0 || kind >= kQedKinds) return fail(HLBL_EINVAL, "hlbl_ctx_set_qed_kernel: bad kind %d", kind);
+#ifdef HLBL_WITH_KQED
+  if (kind == kQedKqed && !c->kq_ready) {
+    // KQED's host set-up (bin/hlbl_hypercube.cpp:174-178), once per context
+    if (initialise(&c->kq) != 0) return fail(HLBL_ECUDA, "hlbl_ctx_set_qed_kernel: KQED initialise failed");
+    c->kq_ready = true;
+  }
+#else
+  if (kind == kQedKqed)
+    return fail(HLBL_EINVAL, "hlbl_ctx_set_qed_kernel: this library was built without KQED (HLBL_KQED_DIR)");
+#endif
   if (c->capturing) return fail(HLBL_ESTATE, "hlbl_ctx_set_qed_kernel: during graph capture");
   if (kind != kQedStandInClosed && c->qed_mode == HLBL_QED_SURROGATE)
     return fail(HLBL_ESTATE, "hlbl_ctx_set_qed_kernel: the learned weight replaces the stand-in's closed form only");

@@ -403,11 +403,23 @@ __device__ __forceinline__ void generic_contract(const Q& prov, const T* a, cons
 
 // Geometry G of every target of the launch, partial sums of this CTA:
 // part[((t * 5 + slot) * pstride + blockIdx.x) * 64 + rho*16 + sigma*4 + nu].
-// FP32: four CTAs per SM (three for G = 3 and its 72 sums); FP64: as many as fit
 // Q: ClosedStandIn (the stand-in's closed form, the weights from p.qp) or a
 // provider (any QED kernel, generic_contract).
+template <class Q>
+constexpr int p234_state() {
+  if constexpr (std::is_same_v<Q, ClosedStandIn>) return 0;
+  else return Q::kState;
+}
+// FP32: four CTAs per SM (three for G = 3 and its 72 sums); FP64 and
+// whole-tensor providers (a linked KQED's device function brings its own
+// register count, which a tighter bound would conflict with): one
 template <typename T, int G, class Q>
-__global__ void __launch_bounds__(kP234Threads, sizeof(T) == 4 ? (G == 3 ? 3 : 4) : 1)
+constexpr int p234_min_ctas() {
+  return (sizeof(T) == 4 && p234_state<Q>() <= 64) ? (G == 3 ? 3 : 4) : 1;
+}
+
+template <typename T, int G, class Q>
+__global__ void __launch_bounds__(kP234Threads, p234_min_ctas<T, G, Q>())
     p234_kernel(P234Args p, Q prov, const T* __restrict__ rec, int pstride, double* __restrict__ part) {
   constexpr int NA = G == 3 ? 72 : 24;
   constexpr int NW = kP234Threads / 32;

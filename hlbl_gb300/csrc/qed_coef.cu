@@ -314,6 +314,10 @@ int coef_init(int nsm) {
   if (!rc) rc = coef_attr<QedDense, float, true>();
   if (!rc) rc = coef_attr<QedDenseKerv, double, false>();
   if (!rc) rc = coef_attr<QedDenseKerv, float, true>();
+#ifdef HLBL_WITH_KQED
+  if (!rc) rc = coef_attr<QedKqed, double, false>();
+  if (!rc) rc = coef_attr<QedKqed, float, true>();
+#endif
   return rc;
 }
 

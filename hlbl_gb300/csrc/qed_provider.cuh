@@ -35,6 +35,9 @@
 #include <type_traits>
 
 #include "contract_kernels.cuh"
+#ifdef HLBL_WITH_KQED
+#include "KQED.h"
+#endif
 
 namespace hg {
 
@@ -44,8 +47,9 @@ enum QedKind {
   kQedStandInGeneric = 1,  // the stand-in through the generic paths
   kQedDense = 2,           // the dense test weight, entry by entry
   kQedDenseKerv = 3,       // the dense test weight as a whole-tensor function
+  kQedKqed = 4,            // a linked KQED's QED_Mkernel_L2 (builds with HLBL_WITH_KQED)
 };
-constexpr int kQedKinds = 4;
+constexpr int kQedKinds = 5;
 
 // entry index of kerv[k][mu][nu][lam]
 __host__ __device__ constexpr int kerv_index(int k, int mu, int nu, int lam) {
@@ -142,6 +146,22 @@ struct DenseKervFn {
 };
 using QedDenseKerv = QedKerv<DenseKervFn>;
 
+#ifdef HLBL_WITH_KQED
+// KQED's own device function (kernels/cuda_lattice.cu:266-275 calls it as
+// QED_Mkernel_L2(0.4, xm, ym, kqed_t, kerv)), linked from libKQED_cuda.a in a
+// relocatable-device-code build; the temps travel by value, as the
+// reference passes them to its kernels (cuda_lattice.cu:816-839).
+struct KqedFn {
+  QED_kernel_temps t;
+  double lambda;
+  __device__ __forceinline__ void operator()(const double a[4], const double b[4],
+                                             double kerv[6][4][4][4]) const {
+    QED_Mkernel_L2(lambda, a, b, t, kerv);
+  }
+};
+using QedKqed = QedKerv<KqedFn>;
+#endif
+
 // What a context passes down: the kind and everything its providers need.
 struct QedSel {
   int kind = kQedStandInClosed;
@@ -150,6 +170,9 @@ struct QedSel {
   double r64 = 0.0;
   const double* t64 = nullptr;
   const float* t32 = nullptr;
+#ifdef HLBL_WITH_KQED
+  QED_kernel_temps kq{};
+#endif
 };
 
 // Host: call f(provider) with the provider of a generic kind.
@@ -157,6 +180,9 @@ template <class F>
 decltype(auto) with_provider(const QedSel& q, F&& f) {
   if (q.kind == kQedDense) return f(QedDense{q.t64, q.t32});
   if (q.kind == kQedDenseKerv) return f(QedDenseKerv{DenseKervFn{q.t64}});
+#ifdef HLBL_WITH_KQED
+  if (q.kind == kQedKqed) return f(QedKqed{KqedFn{q.kq, q.qp.lambda}});
+#endif
   return f(QedStandIn{q.qp, q.qf, q.r64});
 }
 

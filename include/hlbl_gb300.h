@@ -345,6 +345,10 @@ int hlbl_surrogate_eval(hlbl_surrogate* s, const float* feat, int n, float* out)
  *                              by entry
  *   HLBL_QEDK_DENSE_KERV       the same tensor evaluated whole per call, as
  *                              a QED_Mkernel_L2-shaped function is
+ *   HLBL_QEDK_KQED             a linked KQED's QED_Mkernel_L2 (device code of
+ *                              libKQED_cuda.a; a library built with
+ *                              HLBL_KQED_DIR set; HLBL_EINVAL otherwise),
+ *                              KQED's initialise() on first selection
  * The generic paths use no structure of the tensor: a coefficient stage
  * folds the three evaluations per site into 640 coefficients in HBM (FP32
  * or FP64 by the path), which the contraction kernels dot with their F rows,
@@ -352,7 +356,7 @@ int hlbl_surrogate_eval(hlbl_surrogate* s, const float* feat, int n, float* out)
  * weight (hlbl_ctx_set_qed) replaces the stand-in's closed form only.
  * Blocking. No counterpart in the reference (it links one kernel). */
 enum { HLBL_QEDK_STANDIN = 0, HLBL_QEDK_STANDIN_GENERIC = 1, HLBL_QEDK_DENSE = 2,
-       HLBL_QEDK_DENSE_KERV = 3 };
+       HLBL_QEDK_DENSE_KERV = 3, HLBL_QEDK_KQED = 4 };
 int hlbl_ctx_set_qed_kernel(hlbl_ctx* ctx, int kind, uint64_t seed);
 
 /* Pass 2's QED weight: HLBL_QED_EXACT, or HLBL_QED_SURROGATE with `s` and
