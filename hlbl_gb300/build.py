@@ -125,7 +125,7 @@ def build_oracle(force: bool = False) -> str:
         return ORACLE_LIB
     cc = shutil.which("gcc") or "cc"
     tmp = ORACLE_LIB + ".tmp"
-    _run([cc, "-std=c11", "-O2", "-fopenmp", "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"),
+    _run([cc, "-std=c11", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"),
           ORACLE_SRC, "-o", tmp, "-lm"])
     os.replace(tmp, ORACLE_LIB)
     return ORACLE_LIB

@@ -110,3 +110,16 @@ def test_qed_standin_structure():
     o.oracle_qed_weights(0.4, 0.1, 0.3, 0.2, S.vp(w0))
     o.oracle_qed_weights(0.4, 5.0, 0.3, 5.0, S.vp(w1))
     assert np.all(w0 > w1) and np.all(w1 > 0)
+
+
+def test_gaussian_fixture_statistics():
+    """The complex Gaussian fixture (hlbl_gb300_rng.h): mean 0, each real part
+    of variance 1/2, uncorrelated real and imaginary parts, and a normal
+    fourth moment (3/4 for N(0, 1/2))."""
+    g = S.gaussian_block((4, 4, 4, 8), 12345)  # 221,184 values
+    re, im = g[0::2], g[1::2]
+    n = len(re)
+    assert abs(np.mean(g)) < 5 / np.sqrt(2 * n)
+    assert abs(np.var(re) - 0.5) < 0.01 and abs(np.var(im) - 0.5) < 0.01
+    assert abs(np.mean(re * im)) < 0.01
+    assert abs(np.mean(re ** 4) - 0.75) < 0.03

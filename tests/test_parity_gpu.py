@@ -158,7 +158,9 @@ def test_device_fixture_generators(hg):
         torch.cuda.synchronize()
         g = d.cpu().numpy()
         h = S.gaussian_block(lat, 78)
-        assert np.max(np.abs(g - h)) <= 1e-13
+        # bit-identical: the fixture's log and sincos are built from exactly
+        # rounded operations that neither compiler fuses (hlbl_gb300_rng.h)
+        assert np.array_equal(g, h)
         assert abs(np.mean(g)) < 0.1 and abs(np.mean(g * g) - 0.5) < 0.1
 
 
