@@ -78,35 +78,33 @@ __device__ __forceinline__ void tile_sums(const float* __restrict__ Arow, const 
       z = 0;
     }
     ++z;
-    // P[s1][s2] = sum_c conj(B[s1][c]) A[s2][c] for s2 = s1^2 and 3-s1, as
-    // packed FP32 pairs of natural operands: with w = (Re B, Im B),
-    // u = (Re A, Im A) and its swap ux = (Im A, Re A), P1 = sum_c w * u and
-    // P2 = sum_c w * ux give Re P = P1.x + P1.y and Im P = P2.x - P2.y -- two
-    // packed FMAs per (c, s2), with only the A row swapped once per site
-    // (each A component serves two products)
-    float2 Bw[12], Au[12], Ax[12];
+    float A[24], B[24];
 #pragma unroll
     for (int c4 = 0; c4 < 6; ++c4) {
       float4 const a = *reinterpret_cast<const float4*>(Arow + c4 * 64 + s * 4);
       float4 const b = *reinterpret_cast<const float4*>(Brow + c4 * 64 + s * 4);
-      Au[2 * c4] = make_float2(a.x, a.y); Au[2 * c4 + 1] = make_float2(a.z, a.w);
-      Ax[2 * c4] = make_float2(a.y, a.x); Ax[2 * c4 + 1] = make_float2(a.w, a.z);
-      Bw[2 * c4] = make_float2(b.x, b.y); Bw[2 * c4 + 1] = make_float2(b.z, b.w);
+      A[4 * c4] = a.x; A[4 * c4 + 1] = a.y; A[4 * c4 + 2] = a.z; A[4 * c4 + 3] = a.w;
+      B[4 * c4] = b.x; B[4 * c4 + 1] = b.y; B[4 * c4 + 2] = b.z; B[4 * c4 + 3] = b.w;
     }
+    // P[s1][s2] = sum_c conj(B[s1][c]) A[s2][c] for s2 = s1^2 and 3-s1, as
+    // packed FP32 pairs: with y = (Re B, Im B), U = sum_c y Re A and
+    // V = sum_c y Im A (the A part broadcast to both halves), Re P = U.x + V.y
+    // and Im P = V.x - U.y -- two packed FMAs per (c, s2) instead of four
     float pa[4][2], pb[4][2];
 #pragma unroll
     for (int s1 = 0; s1 < 4; ++s1) {
-      float2 a1 = make_float2(0.f, 0.f), a2 = a1, b1 = a1, b2 = a1;
+      float2 ua = make_float2(0.f, 0.f), va = ua, ub = ua, vb = ua;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        int const k = 3 * s1 + c, ka = 3 * (s1 ^ 2) + c, kb = 3 * (3 - s1) + c;
-        a1 = __ffma2_rn(Bw[k], Au[ka], a1);
-        a2 = __ffma2_rn(Bw[k], Ax[ka], a2);
-        b1 = __ffma2_rn(Bw[k], Au[kb], b1);
-        b2 = __ffma2_rn(Bw[k], Ax[kb], b2);
+        float2 const y = make_float2(B[2 * (3 * s1 + c)], B[2 * (3 * s1 + c) + 1]);
+        int const sa = 2 * (3 * (s1 ^ 2) + c), sb = 2 * (3 * (3 - s1) + c);
+        ua = __ffma2_rn(y, make_float2(A[sa], A[sa]), ua);
+        va = __ffma2_rn(y, make_float2(A[sa + 1], A[sa + 1]), va);
+        ub = __ffma2_rn(y, make_float2(A[sb], A[sb]), ub);
+        vb = __ffma2_rn(y, make_float2(A[sb + 1], A[sb + 1]), vb);
       }
-      pa[s1][0] = a1.x + a1.y; pa[s1][1] = a2.x - a2.y;
-      pb[s1][0] = b1.x + b1.y; pb[s1][1] = b2.x - b2.y;
+      pa[s1][0] = ua.x + va.y; pa[s1][1] = va.x - ua.y;
+      pb[s1][0] = ub.x + vb.y; pb[s1][1] = vb.x - ub.y;
     }
     float const z3 = zhs[s][3];
 #pragma unroll

@@ -525,42 +525,34 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
             y[4 * c4] = a.x; y[4 * c4 + 1] = a.y; y[4 * c4 + 2] = a.z; y[4 * c4 + 3] = a.w;
           }
           float d[4][4];  // [mu][pq0 re, pq0 im, pq1 re, pq1 im]
-          // O[s1][s2] = sum_c Y[s1][c] conj(S[s2][c]) as packed FP32 pairs of
-          // natural operands: with w = (Re Y, Im Y), its swap ws = (Im Y, Re Y)
-          // and u = (Re S, Im S), A1 = sum_c w * u and A2 = sum_c ws * u give
-          // Re O = A1.x + A1.y and Im O = A2.x - A2.y -- two packed FMAs per
-          // (c, s2), with only the Y row swapped once (no per-product
-          // broadcast of an S component)
-          float2 yw[12], yx[12];
-#pragma unroll
-          for (int k = 0; k < 12; ++k) {
-            yw[k] = make_float2(y[2 * k], y[2 * k + 1]);
-            yx[k] = make_float2(y[2 * k + 1], y[2 * k]);
-          }
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
             const float* Sr = sm.S[ss][q_in + h] + f32_tile_off(s, 0);
-            float2 xs[12];
+            float x[24];
 #pragma unroll
             for (int c4 = 0; c4 < 6; ++c4) {
               float4 const b = *reinterpret_cast<const float4*>(Sr + c4 * 64);
-              xs[2 * c4] = make_float2(b.x, b.y);
-              xs[2 * c4 + 1] = make_float2(b.z, b.w);
+              x[4 * c4] = b.x; x[4 * c4 + 1] = b.y; x[4 * c4 + 2] = b.z; x[4 * c4 + 3] = b.w;
             }
+            // O[s1][s2] = sum_c Y[s1][c] conj(S[s2][c]), s2 = s1^2 (a) and 3-s1 (b),
+            // as packed FP32 pairs: with w = (Re Y, Im Y), U = sum_c w Re S and
+            // V = sum_c w Im S (the S part broadcast), Re O = U.x + V.y and
+            // Im O = U.y - V.x -- two packed FMAs per (c, s2) instead of four
             float oa[4][2], ob[4][2];
 #pragma unroll
             for (int s1 = 0; s1 < 4; ++s1) {
-              float2 a1 = make_float2(0.f, 0.f), a2 = a1, b1 = a1, b2 = a1;
+              float2 ua = make_float2(0.f, 0.f), va = ua, ub = ua, vb = ua;
 #pragma unroll
               for (int cc = 0; cc < 3; ++cc) {
-                int const k = 3 * s1 + cc, ka = 3 * (s1 ^ 2) + cc, kb = 3 * (3 - s1) + cc;
-                a1 = __ffma2_rn(yw[k], xs[ka], a1);
-                a2 = __ffma2_rn(yx[k], xs[ka], a2);
-                b1 = __ffma2_rn(yw[k], xs[kb], b1);
-                b2 = __ffma2_rn(yx[k], xs[kb], b2);
+                float2 const w = make_float2(y[2 * (3 * s1 + cc)], y[2 * (3 * s1 + cc) + 1]);
+                int const sa = 2 * (3 * (s1 ^ 2) + cc), sb = 2 * (3 * (3 - s1) + cc);
+                ua = __ffma2_rn(w, make_float2(x[sa], x[sa]), ua);
+                va = __ffma2_rn(w, make_float2(x[sa + 1], x[sa + 1]), va);
+                ub = __ffma2_rn(w, make_float2(x[sb], x[sb]), ub);
+                vb = __ffma2_rn(w, make_float2(x[sb + 1], x[sb + 1]), vb);
               }
-              oa[s1][0] = a1.x + a1.y; oa[s1][1] = a2.x - a2.y;
-              ob[s1][0] = b1.x + b1.y; ob[s1][1] = b2.x - b2.y;
+              oa[s1][0] = ua.x + va.y; oa[s1][1] = ua.y - va.x;
+              ob[s1][0] = ub.x + vb.y; ob[s1][1] = ub.y - vb.x;
             }
 #pragma unroll
             for (int mu = 0; mu < 4; ++mu) {
