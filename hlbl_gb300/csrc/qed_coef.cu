@@ -262,6 +262,129 @@ __global__ void __launch_bounds__(kLinThreads, 1)
   }
 }
 
+// The FP32 layout's version of the same stage: the table columns of the
+// thread's two outputs are (n, n + 1) pairs and each basis value is stored
+// twice, (phi, phi), so one packed FMA updates both outputs from one shared
+// load; the code of each warp's output type has its evaluations fixed at
+// compile time, and two sites go through each loop for more independent
+// FMA chains.
+__global__ void __launch_bounds__(kLinThreads, 1)
+    qed_coef_linear32_kernel(Geometry geo, CoefArgs args, const float* __restrict__ tab,
+                             float* __restrict__ out) {
+  __shared__ __align__(16) float2 s_phi[kLinSites][3][kPhiPad];
+  __shared__ float s_zh[kLinSites][4];
+  extern __shared__ __align__(16) float s_stage[];  // one tile's outputs in the layout's order
+  int const t = threadIdx.x, pi = blockIdx.y;
+  int const gsx[4] = {args.batch.p[pi].gsx[0], args.batch.p[pi].gsx[1], args.batch.p[pi].gsx[2],
+                      args.batch.p[pi].gsx[3]};
+  int const yv[4] = {args.batch.p[pi].yv[0], args.batch.p[pi].yv[1], args.batch.p[pi].yv[2],
+                     args.batch.p[pi].yv[3]};
+  float const xu = (float)args.xunit;
+  out += (size_t)pi * args.stride;
+  bool const zht = t >= 192;  // warps 6-9: the zerohalf outputs (uniform per warp)
+  int const mu = zht ? (t - 192) / 32 : t / 48;
+  int const n = zht ? 96 + 2 * ((t - 192) % 32) : 2 * (t % 48);
+  int const lam = n & 3, nu = (n >> 2) & 3, j = n >> 4;
+  float2 tc[3][kLinNB];
+  int zi[3];
+  float zs[3];
+  if (!zht) {
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      int const i0 = q == 0 ? kerv_index(j, mu, nu, lam) : q == 1 ? kerv_index(j, nu, mu, lam) : kerv_index(j, lam, nu, mu);
+      int const i1 = q == 0 ? kerv_index(j, mu, nu, lam + 1)
+                   : q == 1 ? kerv_index(j, nu, mu, lam + 1) : kerv_index(j, lam + 1, nu, mu);
+      float const sg = q == 2 ? -1.f : 1.f;
+#pragma unroll
+      for (int b = 0; b < kLinNB; ++b)
+        tc[q][b] = make_float2(sg * tab[b * HLBL_QED_NK + i0], sg * tab[b * HLBL_QED_NK + i1]);
+      zi[q] = 0;
+      zs[q] = 1.f;
+    }
+  } else {
+    int const tau = j - 6;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      int k = 0, c = 0;
+#pragma unroll
+      for (int kk = 0; kk < 6; ++kk) {
+        bool const m = comb_rho(kk) == tau || comb_sigma(kk) == tau;
+        if (m && c == q) k = kk;
+        c += m ? 1 : 0;
+      }
+      int const r = comb_rho(k), g = comb_sigma(k);
+      zi[q] = g == tau ? r : g;
+      zs[q] = g == tau ? 1.f : -1.f;
+#pragma unroll
+      for (int b = 0; b < kLinNB; ++b)
+        tc[q][b] = make_float2(tab[b * HLBL_QED_NK + kerv_index(k, lam, nu, mu)],
+                               tab[b * HLBL_QED_NK + kerv_index(k, lam + 1, nu, mu)]);
+    }
+  }
+  long long const vpad = (geo.V + kLinSites - 1) / kLinSites * kLinSites;
+  long long const ntiles = vpad / kLinSites;
+  float ym[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) ym[r] = (float)coord_map(mod_pos(yv[r], geo.global[r]), geo.global[r]) * xu;
+  float* const st_base = s_stage + ((mu * (kBtN / 4) + (n >> 2)) * 32) * 4 + (n & 3);
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    long long const s0 = tile * kLinSites;
+    if (t < kLinSites * 3) {
+      int const s = t / 3, e = t % 3;
+      int rel[4];
+      rel_coords(geo, gsx, min(s0 + s, geo.V - 1), rel);
+      float xm[4], xmy[4], a[4], b[4], phi[kPhiPad];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        xm[r] = (float)coord_map(rel[r], geo.global[r]) * xu;
+        xmy[r] = (float)coord_map_diff(rel[r], yv[r], geo.global[r]) * xu;
+        a[r] = e == 1 ? ym[r] : xm[r];
+        b[r] = e == 0 ? ym[r] : (e == 1 ? xm[r] : xmy[r]);
+        if (e == 0) s_zh[s][r] = (float)coord_map_zerohalf(rel[r], geo.global[r]);
+      }
+      dense_basis_t<float>(a, b, phi);
+#pragma unroll
+      for (int i = 0; i < kPhiPad; ++i) s_phi[s][e][i] = make_float2(phi[i], phi[i]);
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int s = 0; s < kLinSites; s += 2) {
+      float2 v[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        float2 acc[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          const float2* ph = &s_phi[s + h][zht ? 2 : q][0];
+          float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int b = 0; b < kLinNB; ++b) a = __ffma2_rn(tc[q][b], ph[b], a);
+          acc[q] = a;
+        }
+        if (zht) {
+          v[h] = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            float const w = zs[q] * s_zh[s + h][zi[q]];
+            v[h] = __ffma2_rn(make_float2(w, w), acc[q], v[h]);
+          }
+        } else {
+          v[h] = make_float2(acc[0].x + acc[1].x + acc[2].x, acc[0].y + acc[1].y + acc[2].y);
+        }
+        if (s0 + s + h >= geo.V) v[h] = make_float2(0.f, 0.f);
+      }
+      *reinterpret_cast<float2*>(st_base + s * 4) = v[0];
+      *reinterpret_cast<float2*>(st_base + (s + 1) * 4) = v[1];
+    }
+    __syncthreads();
+    // the tile's block of the FP32 layout is contiguous
+    float4* dst = reinterpret_cast<float4*>(out + (size_t)tile * kTileCoef);
+    const float4* src = reinterpret_cast<const float4*>(s_stage);
+    for (int i = t; i < kTileCoef / 4; i += kLinThreads) dst[i] = src[i];
+    __syncthreads();
+  }
+}
+
 int g_coef_grid = 0;
 int g_lin_grid = 0;
 
@@ -280,11 +403,12 @@ void coef_run(const P& prov, const Geometry& geo, const CoefArgs& a, int npairs,
     long long const vpad = F32 ? (geo.V + kLinSites - 1) / kLinSites * kLinSites : geo.V;
     long long const ntiles = (vpad + kLinSites - 1) / kLinSites;
     int const grid = (int)std::max<long long>(1, std::min<long long>(ntiles, std::max(1, g_lin_grid / npairs)));
-    const T* tab;
-    if constexpr (sizeof(T) == 8) tab = reinterpret_cast<const T*>(prov.t64);
-    else tab = reinterpret_cast<const T*>(prov.t32);
-    qed_coef_linear_kernel<T, F32><<<dim3(grid, npairs), kLinThreads, F32 ? kTileCoef * sizeof(float) : 0, st>>>(
-        geo, a, tab, out);
+    if constexpr (F32) {
+      qed_coef_linear32_kernel<<<dim3(grid, npairs), kLinThreads, kTileCoef * sizeof(float), st>>>(
+          geo, a, prov.t32, out);
+    } else {
+      qed_coef_linear_kernel<T, F32><<<dim3(grid, npairs), kLinThreads, 0, st>>>(geo, a, prov.t64, out);
+    }
     return;
   }
   constexpr int CS = coef_sites<P, T>();
@@ -299,11 +423,11 @@ void coef_run(const P& prov, const Geometry& geo, const CoefArgs& a, int npairs,
 int coef_init(int nsm) {
   g_coef_grid = nsm * 4;
   {
-    cudaError_t e = cudaFuncSetAttribute(qed_coef_linear_kernel<float, true>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kTileCoef * (int)sizeof(float));
+    cudaError_t e = cudaFuncSetAttribute(qed_coef_linear32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kTileCoef * (int)sizeof(float));
     if (e != cudaSuccess) return cuda_fail(e, "QED coefficient (linear) smem attribute");
     int nb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, qed_coef_linear_kernel<float, true>, kLinThreads,
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, qed_coef_linear32_kernel, kLinThreads,
                                                       kTileCoef * sizeof(float));
     if (e != cudaSuccess) return cuda_fail(e, "QED coefficient (linear) occupancy");
     g_lin_grid = nsm * (nb > 0 ? nb : 1);
