@@ -63,6 +63,9 @@ def parse():
     ap.add_argument("--config5", action="store_true",
                     help="the 48^3x96 host-cache line alone (about 75 GB of pinned host memory)")
     ap.add_argument("--c5-partners", type=int, default=3)
+    ap.add_argument("--config2-chain", action="store_true",
+                    help="the whole 24^3x48 chain (275 pairs) in FP32 and FP64, every pair's error (minutes)")
+    ap.add_argument("--c2-ref-pairs", type=int, default=8)
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="skip the baseline leg of the reference's own kernels on the GPU")
     ap.add_argument("--no-autotune", action="store_true",
@@ -242,6 +245,8 @@ def main():
     torch.cuda.set_device(local_rank)
     if args.config5:
         return run_config5(args, hg, torch, rank)
+    if args.config2_chain:
+        return run_config2_chain(args, hg, torch, rank)
     if args.only_2p2:
         return run_2p2_only(args, hg, torch, rank)
     dist = None
@@ -737,11 +742,44 @@ def main():
             torch, c, hg, block(q), block(p), schedule.mod_pos(q, LATTICE), schedule.site_map_diff(p, q, LATTICE),
             xu, res64[0].cpu().tolist(), res_main[0].cpu().tolist(), schedule.mod_pos(p, LATTICE))
     if rank == 0:
-        print(json.dumps(out), flush=True)
+        print(json.dumps(ordered(out)), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+def ordered(out):
+    """The contract's keys first, then a compact summary of every line (so a
+    reader of a truncated line still has them), then the details."""
+    def g(*path):
+        v = out
+        for k in path:
+            if not isinstance(v, dict) or k not in v:
+                return None
+            v = v[k]
+        return v
+
+    summary = {
+        "headline_pairs_per_s": g("value"), "e2e_pairs_per_s": g("e2e", "value"),
+        "max_rel_err_vs_fp64": g("max_rel_err_vs_fp64"), "chain_total_rel_err_vs_fp64": g("chain_total_rel_err_vs_fp64"),
+        "fp64_pairs_per_s": g("fp64", "value"),
+        "reference_gpu_pairs_per_s": g("reference_gpu_baseline", "kernel_sum", "value"),
+        "cpu_port_pairs_per_s": g("cpu_baseline", "value"),
+        "surrogate": {"pairs_per_s": g("surrogate", "value"), "max_rel_err": g("surrogate", "max_rel_err_vs_fp64"),
+                      "chain_total_rel_err": g("surrogate", "chain_total_rel_err_vs_fp64")},
+        "generic_dense_pairs_per_s": g("generic_qed", "dense", "value"),
+        "chains16_pairs_per_s": g("chains16", "value"),
+        "pieces_2p2_ms_per_source": g("pieces_2p2", "value"),
+        "reference_gpu_2p2_ms_per_source": g("reference_gpu_baseline", "pieces_2p2", "value"),
+        "pass1_ms": g("rooflines", "pass1", "kernel_ms"), "pass2_ms": g("rooflines", "pass2", "kernel_ms"),
+    }
+    first = ["metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+             "vs_baseline", "dtype", "data", "config", "e2e", "roofline", "cpu_baseline", "clocks", "gpu_launches"]
+    res = {k: out[k] for k in first if k in out}
+    res["summary"] = summary
+    res.update({k: v for k, v in out.items() if k not in res})
+    return res
 
 
 def bench_chains16(c, hg, torch, xu, res64_pairs):
@@ -941,6 +979,94 @@ def bench_2p2(c, hg, torch, stream, fwd, x32, gsw, xu, reps):
             "gpu_launches_per_source": 3 + 5 * ((N_TARGETS_2P2 + 31) // 32),
             "reference_readme": "compute_2p2_gpu 4.6 s per 16 targets, one GH200, 262,144 sites, "
                                 "real KQED (not comparable weight)"}
+
+
+def run_config2_chain(args, hg, torch, rank):
+    """The whole 24^3x48 chain (stride 2, h = (+1,-1,+1,-1), K = 4: 76
+    propagators, 275 pairs) through the library's driver twice: the headline
+    path (FP32 tile copies, batched, a graph per window) and the FP64 path pair
+    by pair (the reference's algorithm and loop); every pair's error and the
+    chain totals. Then a sample of pairs by the reference's own kernels built
+    for sm_103a (oracle/ref_gpu, a baseline leg) against the FP64 path."""
+    import platform
+
+    import numpy as np
+
+    from hlbl_gb300 import schedule
+    from hlbl_gb300.cache import PropagatorCache, TorchBuffers
+    from hlbl_gb300.driver import run_chain
+
+    if rank != 0:
+        return 0
+    xu = hg.xunit(MUON_MEV, SPACING_FM)
+    steps = schedule.build_schedule(H, STRIDE, NSTEPS)
+    c = hg.Contractor(LATTICE)
+    stream = torch.cuda.Stream()
+    c.set_stream(stream)
+
+    def provider(site, dest):
+        c.fill_gaussian_block(dest, hg.Contractor.source_seed(RUN_SEED, site))
+
+    def out_factory(n):
+        return torch.zeros((n, 2), dtype=torch.float64, device="cuda")
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r32, st32 = run_chain(steps, LATTICE, xu, provider, c, PropagatorCache("device32", c.block_length, TorchBuffers(c)),
+                          batched=True, graphs=True, out_factory=out_factory)
+    torch.cuda.synchronize()
+    t32 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    r64, st64 = run_chain(steps, LATTICE, xu, provider, c, PropagatorCache("device", c.block_length, TorchBuffers(c)),
+                          precision=hg.FP64)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    ref = {(r.x, r.y): np.array(r.kernel_sum) for r in r64}
+    per_pair = [float(np.max(np.abs(np.array(r.kernel_sum) - ref[(r.x, r.y)])) / np.max(np.abs(ref[(r.x, r.y)])))
+                for r in r32]
+    tot32 = np.sum([r.kernel_sum for r in r32], axis=0)
+    tot64 = np.sum([r.kernel_sum for r in r64], axis=0)
+    scale = np.sum([np.abs(r.kernel_sum) for r in r64], axis=0)
+    out = {"metric": "the 24^3x48 chain (275 pairs): FP32 headline path against FP64, every pair",
+           "pairs": len(r32), "pairs_fp64": len(r64), "propagators": st32.positions_solved,
+           "fp32_path_seconds": round(t32, 2), "fp64_path_seconds": round(t64, 2),
+           "max_rel_err_per_pair": max(per_pair), "median_rel_err_per_pair": float(np.median(per_pair)),
+           "chain_total_rel_err": float(np.max(np.abs(tot32 - tot64) / np.abs(tot64))),
+           "chain_total_err_at_chain_scale": float(np.max(np.abs(tot32 - tot64) / scale)),
+           "chain_totals_fp64": tot64.tolist()}
+    path = os.path.join(ROOT, "oracle", "_ref", "gpu", platform.machine(), "libhlbl_ref_gpu.so")
+    if os.path.exists(path) and args.c2_ref_pairs > 0:
+        lib = C.CDLL(path)
+        I4 = C.c_int * 4
+        vpt = C.c_void_p
+        lib.refgpu_last_error.restype = C.c_char_p
+        lib.refgpu_create.argtypes = [C.POINTER(vpt), I4, C.c_int, C.c_ulonglong]
+        lib.refgpu_destroy.argtypes = [vpt]
+        lib.refgpu_kernel_sum.argtypes = [vpt, vpt, vpt, I4, I4, C.c_double, vpt]
+        lib.refgpu_reserve_kernel_memory.argtypes = [vpt, C.c_int, C.POINTER(C.c_size_t)]
+        h = vpt()
+        assert lib.refgpu_create(C.byref(h), I4(*LATTICE), 0, 0) == 0, lib.refgpu_last_error()
+        nb = C.c_size_t()
+        assert lib.refgpu_reserve_kernel_memory(h, 1, C.byref(nb)) == 0, lib.refgpu_last_error()
+        a = torch.empty(c.block_length, dtype=torch.float64, device="cuda")
+        b = torch.empty(c.block_length, dtype=torch.float64, device="cuda")
+        errs, secs = [], []
+        for r in r64[:args.c2_ref_pairs]:
+            provider(tuple(r.x), a)
+            provider(tuple(r.y), b)
+            stream.synchronize()
+            ks = (C.c_double * 2)()
+            t0 = time.perf_counter()
+            assert lib.refgpu_kernel_sum(h, vpt(a.data_ptr()), vpt(b.data_ptr()), I4(*r.x), I4(*r.yv),
+                                         C.c_double(xu), ks) == 0
+            secs.append(time.perf_counter() - t0)
+            errs.append(float(np.max(np.abs(np.array(r.kernel_sum) - np.array([ks[0], ks[1]])) /
+                                     np.abs(np.array([ks[0], ks[1]])))))
+        lib.refgpu_destroy(h)
+        out["reference_gpu_sample"] = {"pairs": len(errs), "fp64_max_rel_err_vs_reference_kernels": max(errs),
+                                       "reference_seconds_per_pair": round(float(np.mean(secs)), 3)}
+    print(json.dumps(out), flush=True)
+    return 0
 
 
 def run_config5(args, hg, torch, rank):

@@ -215,3 +215,39 @@ def test_surrogate_and_generic_kind_exclude_each_other():
         with pytest.raises(hg.HlblError):
             c.set_qed_kernel(7)
         c.set_qed_kernel(hg.QED_STANDIN)
+
+
+def test_dense_weight_two_rank_site_split():
+    """The reference's domain decomposition with the dense weight: two ranks
+    along t, the pass-1 sums of both added before pass 2 (the all-reduce),
+    each rank's pass 2 on its own sites with the generic coefficients; the
+    ranks' total equals the oracle's one-rank sums of the whole lattice."""
+    import hlbl_gb300 as hg
+
+    glob, loc = (8, 4, 4, 6), (4, 4, 4, 6)
+    gsx, yv, xu = (5, 1, 3, 2), (-2, 1, 0, 3), hg.xunit(105.658, 0.1)
+    seeds = (611, 612)
+    whole = [S.random_block(glob, s) for s in seeds]
+    with S.dense_qed():
+        want = S.oracle_kernel_sum(whole[0], whole[1], gsx, yv, xu, glob)
+    V, Vl = S.volume(glob), S.volume(loc)
+    # t is the slowest site index: rank r holds sites [r Vl, (r + 1) Vl)
+    blocks = {r: [dev(b.reshape(2, 12, V, 24)[:, :, r * Vl:(r + 1) * Vl, :]) for b in whole] for r in (0, 1)}
+    with hg.Contractor(glob, loc, (0, 0, 0, 0)) as c:
+        c.set_qed_kernel(hg.QED_DENSE, S.DENSE_SEED)
+        total = np.zeros(2)
+        for f in (0, 1):
+            d_dzu = torch.zeros(1728, dtype=torch.float64, device="cuda")
+            d_dzsu = torch.zeros(1152, dtype=torch.float64, device="cuda")
+            for r in (0, 1):
+                c.cu_dzu_dzsu(d_dzu, d_dzsu, blocks[r][0], blocks[r][1], f, (r, 0, 0, 0), gsx, glob, loc)
+            d_gu = torch.zeros(6912, dtype=torch.float64, device="cuda")
+            d_gs = torch.zeros(4608, dtype=torch.float64, device="cuda")
+            c.insert_gammas(d_dzu, d_dzsu, d_gu, d_gs)
+            for r in (0, 1):
+                d_ks = torch.zeros(1, dtype=torch.float64, device="cuda")
+                c.cu_4pt_contraction(d_ks, d_gu, d_gs, blocks[r][0], blocks[r][1], f, (r, 0, 0, 0),
+                                     gsx, xu, yv, glob, loc)
+                torch.cuda.synchronize()
+                total[f] += d_ks.item()
+    assert S.rel_err(total, want) <= TOL64, (total, want)

@@ -82,3 +82,43 @@ def test_reference_gpu_pieces_2p2_match_host_emulation_and_library():
             for g in range(5):
                 assert np.max(np.abs(p234[t, g] - ref[t, g])) <= TOL_REF * scale(ref[t, g]), (t, g)
                 assert np.max(np.abs(o234[t, g] - p234[t, g])) <= TOL_REF * scale(p234[t, g]), (t, g)
+
+
+@pytest.mark.parametrize("dense", [False, True], ids=["standin", "dense"])
+def test_config1_chain_matches_reference_kernels(dense):
+    """The 8^3 x 16 chain (stride 1, h = (1,1,1,1), K = 1: 31 propagators, 80
+    pairs x 2 flavours) through the library's driver on the host cache, the
+    reference's loop (each source's pairs right after its solve, FP64), and
+    every pair's sums against the reference's own kernels on the same blocks."""
+    import hlbl_gb300 as hg
+    from hlbl_gb300 import schedule
+    from hlbl_gb300.cache import PropagatorCache, TorchBuffers
+    from hlbl_gb300.driver import run_chain
+
+    lat = (16, 8, 8, 8)
+    xu = hg.xunit(105.658, 0.1)
+    steps = schedule.build_schedule((1, 1, 1, 1), 1, 1)
+    blocks = {}
+
+    def block(site):
+        site = tuple(site)
+        if site not in blocks:
+            blocks[site] = S.gaussian_block(lat, S.source_seed(1234, site))
+        return blocks[site]
+
+    with hg.Contractor(lat) as c:
+        if dense:
+            c.set_qed_kernel(hg.QED_DENSE, S.DENSE_SEED)
+
+        def provider(site, dest):
+            dest.copy_(torch.from_numpy(block(site)))
+
+        res, st = run_chain(steps, lat, xu, provider, c, PropagatorCache("host", c.block_length, TorchBuffers(c)),
+                            precision=hg.FP64)
+    assert len(res) == 80 and st.positions_solved == 31
+    worst = 0.0
+    with S.RefGpu(lat, dense=dense) as r:
+        for p in res:
+            want = r.kernel_sum(dev(block(p.x)), dev(block(p.y)), p.x, p.yv, xu)
+            worst = max(worst, S.rel_err(p.kernel_sum, want))
+    assert worst <= TOL_REF, worst
