@@ -219,11 +219,12 @@ class Contractor:
         return {"p1": ("one stage, 2 CTAs/SM", "two stages, 1 CTA/SM",
                        "one flavour per CTA, two stages, 3 CTAs/SM",
                        "one flavour per CTA, producer warp, empty/full barriers")[v.value],
+                "p1_variant": v.value,
                 "p2": "tensor-core",
                 "batch_group": grp.value, "ms": ms.value}
 
     def set_p1f32_variant(self, variant: int, group: int = 0) -> None:
-        """The FP32-copy path's pass-1 variant (0, 1, 2) and pairs per launch."""
+        """The FP32-copy path's pass-1 variant (0-3, hlbl_gb300.h) and pairs per launch."""
         check(lib.hlbl_ctx_set_p1f32_variant(self._h, int(variant), int(group)))
 
     def f32_tile_copy(self, d_block, d_out) -> None:

@@ -169,3 +169,46 @@ def test_f32_copy_path_matches_oracle_and_fp64_input_path(lat):
         assert S.pair_rel_err(got[i], orc) <= TOL32
         assert S.pair_rel_err(tun[i], orc) <= TOL32
         assert S.pair_rel_err(got[i], r64[i]) <= 1e-5
+
+
+@pytest.mark.parametrize("lat", [(8, 8, 8, 24), (4, 6, 5, 21), (5, 3, 7, 40)])
+def test_f32_copy_pass1_over_many_tiles(lat):
+    """Every pass-1 variant of the FP32-copy path on lattices with several
+    16-site tiles per CTA and runs along z that cross tiles (LZ = 24, 21, 40;
+    odd extents, whose zero-half point is not L/2 of an even L): each pair
+    against the oracle (1e-4) and against the FP64 path at FP32 accuracy
+    (1e-5 at the pair's scale), repeatable bit for bit."""
+    import hlbl_gb300 as hg
+
+    xu = hg.xunit(105.658, 0.1)
+    y = S.gaussian_block(lat, 171)
+    srcs = [S.gaussian_block(lat, 180 + i) for i in range(2)]
+    gsxs = [(1, 2, 3, 5), tuple(L - 1 for L in lat)]
+    yvs = [(1, -1, 2, -3), (0, 2, -1, 7)]
+    with hg.Contractor(lat) as c:
+        d_y, d_srcs = dev(y), [dev(s) for s in srcs]
+        n32 = c.f32_block_length
+        y32 = torch.empty(n32, dtype=torch.float32, device="cuda")
+        x32 = [torch.empty(n32, dtype=torch.float32, device="cuda") for _ in srcs]
+        c.f32_tile_copy(d_y, y32)
+        for d, o in zip(d_srcs, x32):
+            c.f32_tile_copy(d, o)
+        res = {}
+        for v in range(4):
+            c.set_p1f32_variant(v, 1)
+            o = torch.zeros((2, 2), dtype=torch.float64, device="cuda")
+            c.kernel_sums_batched_f32(y32, x32, gsxs, yvs, xu, o)
+            o2 = torch.zeros_like(o)
+            c.kernel_sums_batched_f32(y32, x32, gsxs, yvs, xu, o2)
+            assert torch.equal(o, o2)  # fixed order: repeatable bit for bit
+            res[v] = o.cpu().numpy()
+        r64 = torch.zeros((2, 2), dtype=torch.float64, device="cuda")
+        c.kernel_sums_batched(d_y, d_srcs, gsxs, yvs, xu, r64, hg.FP64)
+        c.check()
+        r64 = r64.cpu().numpy()
+    for i in range(2):
+        orc = S.oracle_kernel_sum(srcs[i], y, gsxs[i], yvs[i], xu, lat)
+        assert S.pair_rel_err(r64[i], orc) <= 1e-12
+        for v in range(4):
+            assert S.pair_rel_err(res[v][i], orc) <= TOL32
+            assert S.pair_rel_err(res[v][i], r64[i]) <= 1e-5, (v, res[v][i], r64[i])
