@@ -339,6 +339,14 @@ __device__ __forceinline__ float epilogue_row_generic(uint32_t lane_addr, uint32
   return a;
 }
 
+// The D formation's closed forms of D_mu from the spin-block products follow
+// from these phases (i^((2 - g5g_ph(mu, s1)) & 3) for s1 = 0..3).
+constexpr int d_ph(int mu, int s1) { return (6 - g5g_ph(mu, s1)) & 3; }
+static_assert(d_ph(0, 0) == 0 && d_ph(0, 1) == 0 && d_ph(0, 2) == 2 && d_ph(0, 3) == 2, "D_0 = a0 + a1 - a2 - a3");
+static_assert(d_ph(3, 0) == 3 && d_ph(3, 1) == 1 && d_ph(3, 2) == 3 && d_ph(3, 3) == 1, "D_3 = i (a1 + a3 - a0 - a2)");
+static_assert(d_ph(1, 0) == 3 && d_ph(1, 1) == 3 && d_ph(1, 2) == 3 && d_ph(1, 3) == 3, "D_1 = -i (b0 + b1 + b2 + b3)");
+static_assert(d_ph(2, 0) == 0 && d_ph(2, 1) == 2 && d_ph(2, 2) == 0 && d_ph(2, 3) == 2, "D_2 = b0 - b1 + b2 - b3");
+
 // ---- the kernel ------------------------------------------------------------------
 // kGeneric: the QED weighting from the coefficient tensor of args.coef (any
 // QED kernel, qed_provider.cuh) instead of the stand-in's closed form.
@@ -498,6 +506,7 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
     int const j = (warp - kWarpD0) % kDGroup;    // the chunk's j-th pair of (p, q)
     int const s = lane;
     bool ok = true;
+    float y[24];  // this lane's Y row p: loaded at a p-block's first chunk, kept for its three
     for (int P = 0; ok && P < nph; ++P) {
       long long const tile = blockIdx.x + (long long)(P >> 1) * gridDim.x;
       int const nvalid = (int)min((long long)kSites, geo.V - tile * kSites);
@@ -517,12 +526,13 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
         float* Ahi = sm.A[as][0] + j * 16 * 32 + s * 4;
         float* Alo = sm.A[as][1] + j * 16 * 32 + s * 4;
         if (s < nvalid) {
-          const float* Yr = sm.Y[ys][p_in] + f32_tile_off(s, 0);
-          float y[24];
+          if (bq == 0) {
+            const float* Yr = sm.Y[ys][p_in] + f32_tile_off(s, 0);
 #pragma unroll
-          for (int c4 = 0; c4 < 6; ++c4) {
-            float4 const a = *reinterpret_cast<const float4*>(Yr + c4 * 64);
-            y[4 * c4] = a.x; y[4 * c4 + 1] = a.y; y[4 * c4 + 2] = a.z; y[4 * c4 + 3] = a.w;
+            for (int c4 = 0; c4 < 6; ++c4) {
+              float4 const a = *reinterpret_cast<const float4*>(Yr + c4 * 64);
+              y[4 * c4] = a.x; y[4 * c4 + 1] = a.y; y[4 * c4 + 2] = a.z; y[4 * c4 + 3] = a.w;
+            }
           }
           float d[4][4];  // [mu][pq0 re, pq0 im, pq1 re, pq1 im]
 #pragma unroll
@@ -531,41 +541,48 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
             float x[24];
 #pragma unroll
             for (int c4 = 0; c4 < 6; ++c4) {
-              float4 const b = *reinterpret_cast<const float4*>(Sr + c4 * 64);
-              x[4 * c4] = b.x; x[4 * c4 + 1] = b.y; x[4 * c4 + 2] = b.z; x[4 * c4 + 3] = b.w;
+              float4 const bb = *reinterpret_cast<const float4*>(Sr + c4 * 64);
+              x[4 * c4] = bb.x; x[4 * c4 + 1] = bb.y; x[4 * c4 + 2] = bb.z; x[4 * c4 + 3] = bb.w;
             }
-            // O[s1][s2] = sum_c Y[s1][c] conj(S[s2][c]), s2 = s1^2 (a) and 3-s1 (b),
+            // O[s1][s2] = sum_c Y[s1][c] conj(S[s2][c]) for s2 = s1^2 (a) and 3-s1 (b),
             // as packed FP32 pairs: with w = (Re Y, Im Y), U = sum_c w Re S and
             // V = sum_c w Im S (the S part broadcast), Re O = U.x + V.y and
-            // Im O = U.y - V.x -- two packed FMAs per (c, s2) instead of four
-            float oa[4][2], ob[4][2];
+            // Im O = U.y - V.x -- two packed FMAs per (c, s2). D_mu = sum_s1
+            // i^((2 - g5g_ph(mu, s1)) & 3) O[s1][s2] (s2 = a for mu = 0, 3; b for
+            // mu = 1, 2), i.e. D_0 = a0 + a1 - a2 - a3, D_3 = i (a1 + a3 - a0 - a2),
+            // D_1 = -i (b0 + b1 + b2 + b3), D_2 = b0 - b1 + b2 - b3: the b
+            // products are summed per parity of s1 inside the FMA chains.
+            float a[4][2];
+            float2 ube = make_float2(0.f, 0.f), vbe = ube, ubo = ube, vbo = ube;
 #pragma unroll
             for (int s1 = 0; s1 < 4; ++s1) {
-              float2 ua = make_float2(0.f, 0.f), va = ua, ub = ua, vb = ua;
+              float2 ua = make_float2(0.f, 0.f), va = ua;
 #pragma unroll
               for (int cc = 0; cc < 3; ++cc) {
                 float2 const w = make_float2(y[2 * (3 * s1 + cc)], y[2 * (3 * s1 + cc) + 1]);
                 int const sa = 2 * (3 * (s1 ^ 2) + cc), sb = 2 * (3 * (3 - s1) + cc);
                 ua = __ffma2_rn(w, make_float2(x[sa], x[sa]), ua);
                 va = __ffma2_rn(w, make_float2(x[sa + 1], x[sa + 1]), va);
-                ub = __ffma2_rn(w, make_float2(x[sb], x[sb]), ub);
-                vb = __ffma2_rn(w, make_float2(x[sb + 1], x[sb + 1]), vb);
+                if (s1 & 1) {
+                  ubo = __ffma2_rn(w, make_float2(x[sb], x[sb]), ubo);
+                  vbo = __ffma2_rn(w, make_float2(x[sb + 1], x[sb + 1]), vbo);
+                } else {
+                  ube = __ffma2_rn(w, make_float2(x[sb], x[sb]), ube);
+                  vbe = __ffma2_rn(w, make_float2(x[sb + 1], x[sb + 1]), vbe);
+                }
               }
-              oa[s1][0] = ua.x + va.y; oa[s1][1] = ua.y - va.x;
-              ob[s1][0] = ub.x + vb.y; ob[s1][1] = ub.y - vb.x;
+              a[s1][0] = ua.x + va.y; a[s1][1] = ua.y - va.x;
             }
-#pragma unroll
-            for (int mu = 0; mu < 4; ++mu) {
-              float dr = 0, di = 0;
-#pragma unroll
-              for (int s1 = 0; s1 < 4; ++s1) {
-                float const* o = (mu == 0 || mu == 3) ? oa[s1] : ob[s1];
-                float vr, vi;
-                mul_iph((6 - g5g_ph(mu, s1)) & 3, o[0], o[1], vr, vi);
-                dr += vr; di += vi;
-              }
-              d[mu][2 * h] = dr; d[mu][2 * h + 1] = di;
-            }
+            float const ber = ube.x + vbe.y, bei = ube.y - vbe.x;
+            float const bor = ubo.x + vbo.y, boi = ubo.y - vbo.x;
+            float const a01r = a[0][0] + a[1][0], a01i = a[0][1] + a[1][1];
+            float const a23r = a[2][0] + a[3][0], a23i = a[2][1] + a[3][1];
+            float const a13r = a[1][0] + a[3][0], a13i = a[1][1] + a[3][1];
+            float const a02r = a[0][0] + a[2][0], a02i = a[0][1] + a[2][1];
+            d[0][2 * h] = a01r - a23r; d[0][2 * h + 1] = a01i - a23i;
+            d[3][2 * h] = a02i - a13i; d[3][2 * h + 1] = a13r - a02r;  // i (a13 - a02)
+            d[1][2 * h] = bei + boi;   d[1][2 * h + 1] = -(ber + bor);  // -i (be + bo)
+            d[2][2 * h] = ber - bor;   d[2][2 * h + 1] = bei - boi;
           }
 #pragma unroll
           for (int mu = 0; mu < 4; ++mu) {
