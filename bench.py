@@ -660,7 +660,7 @@ def main():
                  "p2_fp64_tflops": round(gemm_flop_pair / (p2ms64 / max(1, p2n64) * 1e-3) / 1e12, 4)},
         "speedup_vs_fp64": round(value / (n64 / (ms64 * 1e-3)), 2),
         "surrogate": {"value": round(nsur / (mssur * 1e-3), 4), "unit": "pairs/s",
-                      "path": "the headline path with the MLP weight (exact FP64 outside its validated region)",
+                      "path": "the headline path with the MLP weight (the exact weight outside its validated region: FP32 quadrature, FP64 within 0.1/m_mu of the origin)",
                       "max_rel_err_vs_fp64": rel_sur, "chain_total_rel_err_vs_fp64": chain_sur,
                       "max_rel_err_per_flavour_vs_fp64": rel_sur_fl,
                       "train": train_rep, "fallback_rows_timed": fallbacks,

@@ -28,8 +28,8 @@ namespace hg {
 namespace sur {
 // surrogate.cu: pass 2's weights from the learned surrogate
 int launch_surrogate_weights(const hlbl_surrogate* s, const Geometry& geo, const WArgs& wa,
-                             double r0, double* d_w, unsigned long long* d_fallback,
-                             cudaStream_t st, int nsm);
+                             double r0, const QedF32& qf, double r64, double* d_w,
+                             unsigned long long* d_fallback, cudaStream_t st, int nsm);
 double surrogate_r0(const hlbl_surrogate* s);
 }  // namespace sur
 }  // namespace hg
@@ -395,8 +395,8 @@ int run_weights(hlbl_ctx* c, const Geometry& geo, const PairBatch& b, double xun
   wa.xunit = xunit;
   wa.qp = c->qp;
   if (c->qed_mode == HLBL_QED_SURROGATE)
-    return sur::launch_surrogate_weights(c->sur, geo, wa, c->sur_r0, c->d_w, c->d_fallback, c->stream,
-                                         c->nsm);
+    return sur::launch_surrogate_weights(c->sur, geo, wa, c->sur_r0, c->qf, c->qed_fp32 ? c->qed_r64 : 1e300,
+                                         c->d_w, c->d_fallback, c->stream, c->nsm);
   long long const n = geo.V * 3;
   int const blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)c->nsm * 16 / b.n));
   if (precision == HLBL_FP32 && c->qed_fp32) {

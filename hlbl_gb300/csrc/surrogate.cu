@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "contract_kernels.cuh"
+#include "qed_f32.cuh"
 #include "hlbl_gb300.h"
 #include "hlbl_gb300_rng.h"
 #include "hlbl_internal.h"
@@ -284,6 +285,8 @@ struct InferSmem {
   float sigma[8];
   float feat[8][16][4];   // per warp, 16 rows: u0, u1, u2
   float outv[8][16][8];   // per warp, 16 rows: net outputs
+  float feat32[8][32][4];  // per warp, one row per lane (pass 2's weights)
+  float out32[8][32][8];
 };
 
 __global__ void pack_weights_kernel(const float* __restrict__ p, __nv_bfloat16* __restrict__ wb) {
@@ -411,59 +414,122 @@ infer_rows_kernel(int n, const float* __restrict__ feat, const float* __restrict
 }
 
 // The surrogate QED weights of pass 2 (drop-in for qed_weights_exact_kernel):
-// row = (site, evaluation); inside the fallback radius, the exact weight.
-__global__ void __launch_bounds__(256)
+// a lane per site, its three evaluations one after another. The invariants
+// come from exact integer sums (the arguments are small integer vectors times
+// xunit; correctly rounded FP32 square roots and division, as the FP32 exact
+// weight has them); per evaluation the warp's 32 rows go through the network
+// as two 16-row tiles. Outside the validated region [r0, r1] the exact weight,
+// as the FP32 path's exact weight has it: the FP32 quadrature (correctly
+// rounded division, square root and expf) where min(|a|, |b|) >= r64, and
+// within r64 of the origin the FP64 weight of the FP64 invariants, the warp
+// sharing each such evaluation (one quadrature node per lane), so that no
+// lane's FP64 quadrature holds its warp.
+__device__ __forceinline__ float envelope_f(float M) {
+  float const q = M / (M + 7.8f);
+  return q * q * q * q * q + 1e-6f;
+}
+
+__global__ void __launch_bounds__(256, 2)
 qed_weights_surrogate_kernel(Geometry geo, WArgs args, const float* __restrict__ p,
                              const __nv_bfloat16* __restrict__ wb, const float* __restrict__ sigma,
-                             float R, double r0, double r1, double* __restrict__ w,
+                             float R, double r0, double r1, QedF32 qf, double r64, double* __restrict__ w,
                              unsigned long long* __restrict__ n_fallback) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
   load_infer_smem(S, p, wb, sigma);
   int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  long long const n = geo.V * 3;
   int const pi = blockIdx.y;
+  float const r64f = (float)r64;
   int const gsx[4] = {args.batch.p[pi].gsx[0], args.batch.p[pi].gsx[1], args.batch.p[pi].gsx[2], args.batch.p[pi].gsx[3]};
   int const yv[4] = {args.batch.p[pi].yv[0], args.batch.p[pi].yv[1], args.batch.p[pi].yv[2], args.batch.p[pi].yv[3]};
-  w += (size_t)pi * n * HLBL_QED_NW;
-  long long const nwarps_total = (long long)gridDim.x * (blockDim.x >> 5);
-  unsigned long long fb = 0;
-  for (long long base = ((long long)blockIdx.x * (blockDim.x >> 5) + warp) * 16; base < n;
-       base += nwarps_total * 16) {
-    double X = 0, c = 0, Y = 0;
-    long long const row = base + (lane & 15);
-    if (lane < 16) {
-      if (row < n) {
-        double a[4], b[4];
-        qed_args(geo, gsx, yv, args.xunit, row / 3, (int)(row % 3), a, b);
-        hlbl_qed_invariants(a, b, &X, &c, &Y);
-      }
-      S.feat[warp][lane][0] = (float)(2.0 * X / R - 1.0);
-      S.feat[warp][lane][1] = (float)c;
-      S.feat[warp][lane][2] = (float)(2.0 * Y / R - 1.0);
-    }
-    __syncwarp();
-    warp_mlp(S, S.feat[warp], S.outv[warp]);
-    __syncwarp();
-    if (lane < 16 && row < n) {
-      double* o = w + (size_t)row * HLBL_QED_NW;
-      if (fmin(X, Y) < r0 || fmax(X, Y) > r1) {
-        double ex[HLBL_QED_NW];
-        hlbl_qed_weights(&args.qp, X, c, Y, ex);
-        for (int j = 0; j < NOUT; ++j) o[j] = ex[j];
-        ++fb;
-      } else {
-        float bw[NOUT];
-        base_weights((float)X, (float)c, (float)Y, (float)args.qp.lambda, bw);
-        float const env = (float)envelope(fmax(X, Y));
-        for (int j = 0; j < NOUT; ++j)
-          o[j] = (double)(bw[j] * __expf(S.sigma[j] * S.outv[warp][lane][j] * env));
-      }
-    }
-    __syncwarp();
+  w += (size_t)pi * geo.V * 3 * HLBL_QED_NW;
+  unsigned const V = (unsigned)geo.V, stride = gridDim.x * blockDim.x;
+  float const xuf = (float)args.xunit, r0f = (float)r0, r1f = (float)r1;
+  int iy[4], ny = 0;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    iy[r] = coord_map(mod_pos(yv[r], geo.global[r]), geo.global[r]);
+    ny += iy[r] * iy[r];
   }
-  if (n_fallback && lane < 16) {
-    for (int o = 8; o > 0; o >>= 1) fb += __shfl_down_sync(0x0000ffffu, fb, o, 16);
+  unsigned long long fb = 0;
+  // every lane runs every iteration (the network and the FP64 evaluations are
+  // warp-wide); lanes past the end compute on the last site and store nothing
+  for (unsigned base = blockIdx.x * blockDim.x; base < V; base += stride) {
+    unsigned const site = min(base + threadIdx.x, V - 1);
+    bool const valid = base + threadIdx.x < V;
+    unsigned s = site;
+    int c[4];
+    c[3] = (int)(s % (unsigned)geo.local[3]); s /= (unsigned)geo.local[3];
+    c[2] = (int)(s % (unsigned)geo.local[2]); s /= (unsigned)geo.local[2];
+    c[1] = (int)(s % (unsigned)geo.local[1]); s /= (unsigned)geo.local[1];
+    c[0] = (int)s;
+    int ix[4], ixy[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      int const G = geo.global[r];
+      int const rel = (c[r] + geo.pc[r] * geo.local[r] - gsx[r] + G) % G;
+      ix[r] = coord_map(rel, G);
+      ixy[r] = coord_map_diff(rel, yv[r], G);
+    }
+    int nx = 0, nxy = 0, dxy = 0, dxx = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      nx += ix[r] * ix[r];
+      nxy += ixy[r] * ixy[r];
+      dxy += ix[r] * iy[r];
+      dxx += ix[r] * ixy[r];
+    }
+#pragma unroll 1
+    for (int e = 0; e < 3; ++e) {
+      // e = 0: K(xm, ym), e = 1: K(ym, xm), e = 2: K(xm, x - y)
+      int const na = e == 1 ? ny : nx, nb = e == 0 ? ny : (e == 1 ? nx : nxy), nab = e == 2 ? dxx : dxy;
+      float const ra = sqrtf((float)na), rb = sqrtf((float)nb);
+      float const X = xuf * ra, Y = xuf * rb;
+      float cc = (na > 0 && nb > 0) ? (float)nab / (ra * rb) : 0.f;
+      cc = fminf(1.f, fmaxf(-1.f, cc));
+      S.feat32[warp][lane][0] = 2.f * X / R - 1.f;
+      S.feat32[warp][lane][1] = cc;
+      S.feat32[warp][lane][2] = 2.f * Y / R - 1.f;
+      __syncwarp();
+      warp_mlp(S, S.feat32[warp], S.out32[warp]);
+      warp_mlp(S, S.feat32[warp] + 16, S.out32[warp] + 16);
+      __syncwarp();
+      bool const outside = fminf(X, Y) < r0f || fmaxf(X, Y) > r1f;
+      bool const near = outside && fminf(X, Y) < r64f;
+      double ww[HLBL_QED_NW];
+      if (!outside) {
+        float bw[NOUT];
+        base_weights(X, cc, Y, (float)args.qp.lambda, bw);
+        float const env = envelope_f(fmaxf(X, Y));
+#pragma unroll
+        for (int j = 0; j < NOUT; ++j) ww[j] = (double)(bw[j] * __expf(S.sigma[j] * S.out32[warp][lane][j] * env));
+      } else {
+        float wf[HLBL_QED_NW];
+        if (qf.geometric) weights_f32<true, false>(qf, X, cc, Y, wf);
+        else weights_f32<false, false>(qf, X, cc, Y, wf);
+#pragma unroll
+        for (int j = 0; j < HLBL_QED_NW; ++j) ww[j] = (double)wf[j];
+      }
+      double Xd = 0, cd = 0, Yd = 0;
+      if (near) {
+        Xd = args.xunit * sqrt((double)na);
+        Yd = args.xunit * sqrt((double)nb);
+        cd = (na > 0 && nb > 0) ? (double)nab / sqrt((double)na * (double)nb) : 0.0;
+        cd = cd > 1.0 ? 1.0 : (cd < -1.0 ? -1.0 : cd);
+      }
+      unsigned const m = __ballot_sync(0xffffffffu, near);
+      if (m) qed_weights_fp64_warp(args.qp, m, Xd, cd, Yd, ww);
+      if (valid) {
+        fb += outside ? 1 : 0;
+#pragma unroll
+        for (int j = 0; j < HLBL_QED_NW; ++j) w[((size_t)site * 3 + e) * HLBL_QED_NW + j] = ww[j];
+      }
+      __syncwarp();
+    }
+  }
+  if (n_fallback) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) fb += __shfl_down_sync(0xffffffffu, fb, o);
     if (lane == 0 && fb) atomicAdd(n_fallback, fb);
   }
 }
@@ -675,8 +741,8 @@ namespace sur {
 
 // Pass 2's weights from the surrogate (the launch used by capi.cu).
 int launch_surrogate_weights(const hlbl_surrogate* s, const Geometry& geo, const WArgs& wa,
-                             double r0, double* d_w, unsigned long long* d_fallback,
-                             cudaStream_t st, int nsm) {
+                             double r0, const QedF32& qf, double r64, double* d_w,
+                             unsigned long long* d_fallback, cudaStream_t st, int nsm) {
   double const r1 = s->r1 > 0 ? s->r1 : (double)s->R;
   static bool attr = false;
   size_t const smem = infer_smem_bytes();
@@ -686,11 +752,10 @@ int launch_surrogate_weights(const hlbl_surrogate* s, const Geometry& geo, const
     if (e != cudaSuccess) return cuda_fail(e, "surrogate smem attribute");
     attr = true;
   }
-  long long const rows = geo.V * 3;
   int const blocks = (int)std::max<long long>(
-      1, std::min<long long>((rows + 127) / 128, (long long)nsm * 2 / wa.batch.n));
+      1, std::min<long long>((geo.V + 255) / 256, (long long)nsm * 2 / wa.batch.n));
   qed_weights_surrogate_kernel<<<dim3(blocks, wa.batch.n), 256, smem, st>>>(geo, wa, s->d_p, s->d_wb, s->d_sigma, s->R,
-                                                          r0, r1, d_w, d_fallback);
+                                                          r0, r1, qf, r64, d_w, d_fallback);
   return HLBL_OK;
 }
 

@@ -362,8 +362,11 @@ int hlbl_ctx_set_qed_kernel(hlbl_ctx* ctx, int kind, uint64_t seed);
 /* Pass 2's QED weight: HLBL_QED_EXACT, or HLBL_QED_SURROGATE with `s` and
  * fallback radius r0 (r0 < 0: the radius the training validation chose). */
 int hlbl_ctx_set_qed(hlbl_ctx* ctx, int mode, hlbl_surrogate* s, double r0);
-/* (site, evaluation) rows that pass 2 evaluated exactly inside r0, summed
- * since the mode was set. */
+/* (site, evaluation) rows that pass 2 evaluated exactly, outside the
+ * surrogate's validated region (within r0 of the origin or beyond the
+ * largest radius its validation accepted), summed since the mode was set.
+ * Those rows get the exact weight as the FP32 path has it (hlbl_ctx_set_qed_fp32):
+ * the FP32 quadrature away from the origin, FP64 within r64 of it. */
 int hlbl_ctx_qed_fallbacks(hlbl_ctx* ctx, unsigned long long* n);
 
 /* Measurement hooks. With profiling on, the context times every pass-1 and
