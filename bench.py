@@ -602,6 +602,13 @@ def main():
     p2_avg_ms = p2ms / max(1, p2n)
     p1_avg_ms = p1ms / max(1, p1n)
     traffic = load_traffic()
+    # the committed DRAM traffic is one pair's launch at 24^3 x 48 (V = 663,552);
+    # the rows of the tile copies are read once, so it scales with the sites
+    # and the pairs a launch covers
+    def traffic_per_launch(key, launches):
+        if not traffic or traffic.get(key) is None:
+            return None
+        return round(traffic[key] * (V / 663552) * (n_prof / max(1, launches)))
     # pass 1, per launch of g pairs: both FP64 blocks read (y once, each
     # partner once) and their FP32 tile copies written (half the bytes)
     p1_bytes = sum((1 + gi) for gi in groups) * blk * 0.5 / max(1, p1n)  # FP32 copies read
@@ -614,13 +621,13 @@ def main():
     rl_p1 = {"bound": "hbm", "kernel": f"pass 1 on FP32 tile copies, p1f32_kernel ({tune['p1']}, batched)",
              "achieved": round(p1_gbs, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
              "frac": round(p1_gbs / peaks["hbm_gbs"], 5),
-             "traffic": (traffic or {}).get("p1_bytes_per_launch"),
+             "traffic": traffic_per_launch("p1_bytes_per_launch", p1n),
              "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
              "kernel_ms": round(p1_avg_ms, 3), "bytes_per_launch": p1_bytes}
     rl_p2 = {"bound": "tensor", "kernel": f"pass 2, {tune['p2']} (batched)",
              "achieved": round(p2_tflops, 2), "peak": round(tf32_peak, 1), "unit": "TFLOP/s",
              "frac": round(p2_tflops / tf32_peak, 5),
-             "traffic": (traffic or {}).get("p2_bytes_per_launch"),
+             "traffic": traffic_per_launch("p2_bytes_per_launch", p2n),
              "peak_source": "measured here: cuBLAS TF32 GEMM 8192^3 (torch.matmul, allow_tf32)",
              "issued_tf32_tflops": round(3 * p2_tflops, 2), "kernel_ms": round(p2_avg_ms, 3),
              "hbm_gbs": round(p2_bytes / (p2_avg_ms * 1e-3) / 1e9, 2)}
