@@ -69,6 +69,7 @@ def _load() -> C.CDLL:
                                                C.c_double, C.c_int, vp]),
         "hlbl_ctx_set_batch_group": (C.c_int, [vp, C.c_int]),
         "hlbl_ctx_set_tensor_cores": (C.c_int, [vp, C.c_int]),
+        "hlbl_ctx_set_tc_fp16": (C.c_int, [vp, C.c_int]),
         "hlbl_f32_tile_copy": (C.c_int, [vp, vp, vp]),
         "hlbl_f32_block_length": (C.c_size_t, [vp]),
         "hlbl_kernel_sums_batched_f32": (C.c_int, [vp, vp, C.c_int, C.POINTER(vp), i4p, i4p, C.c_double, vp]),

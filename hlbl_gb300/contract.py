@@ -235,6 +235,10 @@ class Contractor:
         """FP32 two-flavour pass 2 on the tensor cores (default) or the CUDA cores."""
         check(lib.hlbl_ctx_set_tensor_cores(self._h, 1 if on else 0))
 
+    def set_tc_fp16(self, on: bool = True) -> None:
+        """FP16 (on) or TF32 operands in the FP32-copy path's tensor-core pass 2."""
+        check(lib.hlbl_ctx_set_tc_fp16(self._h, 1 if on else 0))
+
     def graph_begin(self) -> None:
         check(lib.hlbl_graph_begin(self._h))
 

@@ -118,15 +118,23 @@ __global__ void f32_tile_copy_kernel(const double* __restrict__ blk, Geometry ge
   int const row = blockIdx.y;
   const double* __restrict__ src_row = blk + (size_t)row * geo.V * 24;
   float* __restrict__ dst_row = out + (size_t)row * nt32 * (32 * 24);
+  float m = 0.f;  // the largest magnitude this thread converts
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     unsigned const lane = i & 31, k = i >> 5, c4 = k % 6, t32 = k / 6;
     unsigned const site = t32 * 32 + lane;
     if (site >= V) continue;  // the copy's padding past the last site is never read
     const double2* src = reinterpret_cast<const double2*>(src_row + (size_t)site * 24 + 4 * c4);
     double2 const v0 = src[0], v1 = src[1];
-    *reinterpret_cast<float4*>(dst_row + (size_t)t32 * (32 * 24) + f32_tile_off((int)lane, (int)c4)) =
-        make_float4(f64_to_f32(v0.x), f64_to_f32(v0.y), f64_to_f32(v1.x), f64_to_f32(v1.y));
+    float4 const f = make_float4(f64_to_f32(v0.x), f64_to_f32(v0.y), f64_to_f32(v1.x), f64_to_f32(v1.y));
+    *reinterpret_cast<float4*>(dst_row + (size_t)t32 * (32 * 24) + f32_tile_off((int)lane, (int)c4)) = f;
+    m = fmaxf(m, fmaxf(fmaxf(fabsf(f.x), fabsf(f.y)), fmaxf(fabsf(f.z), fabsf(f.w))));
   }
+  // the flavour's largest magnitude into the copy's trailer (zeroed before
+  // the launch; non-negative floats order as their bit patterns)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.f)
+    atomicMax(reinterpret_cast<int*>(out + f32_tile_floats(geo.V)) + row / 12, __float_as_int(m));
 }
 
 // ---- launch plumbing -------------------------------------------------------
@@ -233,6 +241,8 @@ struct hlbl_ctx {
   float* d_x32 = nullptr;     // FP32 tile copies: [1 + pair][f32 block] (y first)
   size_t x32_floats = 0;
   float* d_btu = nullptr;     // tensor-core B operand [kMaxBatch][tc_btu_floats_per_pair]
+  float* d_bscale = nullptr;  // FP16 operands: B scale [kMaxBatch][2]
+  int tc16 = 1;               // FP16 operands in the FP32-copy path's pass 2 (hlbl_ctx_set_tc_fp16)
   // staging of host blocks on a side stream (hlbl_stage_async)
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t stage_ev = nullptr;
@@ -368,7 +378,7 @@ int run_pass1(hlbl_ctx* c, const Geometry& geo, const double* y, const PairBatch
   g_build_kernel<<<dim3((kGLen / 2 + 255) / 256, nf, b.n), 256, 0, c->stream>>>(c->d_dz, nf, c->d_g);
   dim3 const gb((kBtK * kBtN + 255) / 256, nf, b.n);
   if (tcp)
-    tc_launch_btu(c->d_g, b.n, c->d_btu, c->stream);
+    tc_launch_btu(c->d_g, b.n, c->d_btu, false, nullptr, c->stream);
   else if (precision == HLBL_FP64)
     bt_build_kernel<double><<<gb, 256, 0, c->stream>>>(c->d_g, c->d_g + kGDzuLen, kGLen,
                                                        (size_t)nf * kGLen, nf, static_cast<double*>(c->d_bt));
@@ -483,7 +493,7 @@ int run_pass2(hlbl_ctx* c, const Geometry& geo, const double* y, const PairBatch
       for (int r = 0; r < 4; ++r) { tb.gsx[i][r] = b.p[i].gsx[r]; tb.yv[i][r] = b.p[i].yv[r]; }
     }
     grid = per_pair_grid(c->grid_tc, b.n, tc_tiles(geo.V));
-    tc_launch_p2(grid, b.n, c->stream, tb, geo, a, c->d_btu, c->d_part2, c->d_err);
+    tc_launch_p2(grid, b.n, c->stream, tb, geo, a, c->d_btu, false, nullptr, c->d_part2, c->d_err);
   } else {
     const float* bt = static_cast<const float*>(c->d_bt);
     if (nf == 2 && c->p2_small) { grid = per_pair_grid(c->grid_p2f2s, b.n, P2F2s::tiles(geo.V)); P2F2s::launch(grid, c->stream, y, b, geo, a, bt, c->d_part2, c->d_err); }
@@ -513,14 +523,14 @@ int run_group_f32(hlbl_ctx* c, const PairBatch& b, const TcBatch& tb, double xun
   p1_reduce_kernel<<<dim3((kDzLen + kRedOut - 1) / kRedOut, 2, b.n), kRedOut * kRedGrp, 0, c->stream>>>(c->d_part1, g1, 2, c->d_dz,
                                                                              nullptr, nullptr);
   g_build_kernel<<<dim3((kGLen / 2 + 255) / 256, 2, b.n), 256, 0, c->stream>>>(c->d_dz, 2, c->d_g);
-  tc_launch_btu(c->d_g, b.n, c->d_btu, c->stream);
+  tc_launch_btu(c->d_g, b.n, c->d_btu, c->tc16 != 0, c->d_bscale, c->stream);
   P2Args a{};
   if (int rc = run_qed(c, geo, b, xunit, HLBL_FP32, a)) return rc;
   a.xunit = xunit;
   a.f0 = 0;
   int const g2 = per_pair_grid(c->grid_tc, b.n, tc_tiles(geo.V));
   prof_begin(c, 1);
-  tc_launch_p2(g2, b.n, c->stream, tb, geo, a, c->d_btu, c->d_part2, c->d_err);
+  tc_launch_p2(g2, b.n, c->stream, tb, geo, a, c->d_btu, c->tc16 != 0, c->d_bscale, c->d_part2, c->d_err);
   prof_end(c, 1);
   p2_reduce_kernel<<<b.n, 64, 0, c->stream>>>(c->d_part2, g2, 2, b, 0);
   return HLBL_OK;
@@ -601,6 +611,7 @@ int hlbl_ctx_create(hlbl_ctx** out, const int global[4], const int local[4],
       {(void**)&c->d_g, sizeof(double) * kMaxBatch * 2 * kGLen},
       {(void**)&c->d_bt, sizeof(double) * kMaxBatch * 2 * kBtK * kBtN},
       {(void**)&c->d_btu, sizeof(float) * kMaxBatch * tc_btu_floats_per_pair()},
+      {(void**)&c->d_bscale, sizeof(float) * kMaxBatch * 2},
       {(void**)&c->d_out, sizeof(double) * 2},
       {(void**)&c->d_err, sizeof(int)}};
   for (auto& b : bufs) {
@@ -625,6 +636,7 @@ void hlbl_ctx_destroy(hlbl_ctx* c) {
   cudaFree(c->d_g);
   cudaFree(c->d_bt);
   cudaFree(c->d_btu);
+  cudaFree(c->d_bscale);
   cudaFree(c->d_x32);
   cudaFree(c->d_out);
   cudaFree(c->d_err);
@@ -806,8 +818,16 @@ int hlbl_f32_tile_copy(hlbl_ctx* c, const double* d_block, float* d_out) {
     if (e != cudaSuccess) return cuda_fail(e, "wait for staged block");
     c->stage_pending = false;
   }
+  cudaError_t e = cudaMemsetAsync(d_out + f32_tile_floats(c->geo.V), 0, kF32Trailer * sizeof(float), c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "hlbl_f32_tile_copy trailer");
   f32_tile_copy_kernel<<<dim3(std::max(1, c->nsm * 8 / 24), 24), 256, 0, c->stream>>>(d_block, c->geo, d_out);
   return check_launch("hlbl_f32_tile_copy launch");
+}
+
+int hlbl_ctx_set_tc_fp16(hlbl_ctx* c, int on) {
+  if (!c) return fail(HLBL_EINVAL, "hlbl_ctx_set_tc_fp16: null context");
+  c->tc16 = on ? 1 : 0;
+  return HLBL_OK;
 }
 
 int hlbl_ctx_set_qed_fp32(hlbl_ctx* c, int on, double r64) {

@@ -43,6 +43,7 @@
 // block (x32/y32: [f][ia][tile][2][6][16][4] floats, f32_tile_off: a site's
 // 24 components as six 16-byte groups, 32 sites per tile in two halves), so
 // pass 2 reads half the bytes of the FP64 blocks and converts nothing.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -60,22 +61,20 @@ constexpr int kSites = 32;                 // sites per tile
 constexpr int kM = 128;                    // MMA rows: (mu, site)
 constexpr int kKc = 16;                    // K per chunk
 constexpr int kChunks = kBtK / kKc;        // 18
-// A and B rings of the same depth, released by one commit per chunk: the
-// tensor pipe's completion reaches the waiting producers about 2,500 cycles
-// after a chunk is issued, so four chunks (about 2,400 cycles of MMAs) must
-// be in flight to keep it busy.
-constexpr int kAStages = 5, kBStages = 5;
-// equal depths: one commit per chunk frees the A and the B stage (a deeper
-// ring for one of them with a second commit per chunk measured slower)
-constexpr bool kSharedEmpty = kAStages == kBStages;
+// A and B rings of the same depth (OpT::kStages: 5 for TF32 operands, 10 for
+// FP16), released by one commit per chunk: the tensor pipe's completion
+// reaches the waiting producers about 2,500 cycles after a chunk is issued, so
+// several chunks must be in flight to keep it busy; one commit per chunk frees
+// the A and the B stage (a deeper ring for one of them with a second commit
+// per chunk measured slower).
 // K order: blocks of 4 p x 4 q (two chunks each), q-blocks inner, so both row
 // sets stream through small rings instead of one being held for a whole
 // phase: the S rows 4 bq..4 bq+3 of a block (a ring of two blocks; fetched
 // again, from L2, for each p-block) and the Y rows of a p-block by halves,
 // half h (rows 4 bp + 2h, 4 bp + 2h + 1) read only by D group h (a ring of
 // three halves). This leaves room for five A and B stages.
-constexpr int kRowsPerGroup = 4, kSGroups = 2, kBlocksQ = 3;
-constexpr int kYRows = 2, kYSlots = 3;
+constexpr int kRowsPerGroup = 4, kBlocksQ = 3;
+constexpr int kYRows = 2;
 constexpr int kBlocks = 9;  // per phase: 3 p-blocks x 3 q-blocks
 constexpr int kHalf = kChunks / 2;               // chunks per main-accumulator half
 constexpr uint32_t kCorrCol = 2 * kBtN;          // the correction accumulator's first column
@@ -88,24 +87,77 @@ constexpr int kThreads = 32 * (kWarpE0 + kEWarps);
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kRowBytes = kRowF32 * 4;  // 3072
 
-// instruction descriptor, kind::tf32: D F32, A and B TF32, both K-major,
+// Operand type of the products (both TF32 or both FP16; D is F32 either way).
+// FP16: the same 3-term split as TF32 (hi = the rounding of the value, lo =
+// the rounding of the rest: 11 + 11 significant bits) in half the bytes, with
+// one MMA of K = 16 per product and chunk instead of two of K = 8, so the
+// rings hold twice the chunks. FP16's exponent range is met by power-of-two
+// scales: A by 2^(15 - e) with 2^e above the bound 24 max|Y| max|S| of every
+// D value (from the per-flavour maxima the tile copies carry), B by the same
+// rule from max|Bt| per pair and flavour; the epilogue divides each row's dot
+// by the product (exact). The bytes saved go to deeper row rings (four S
+// blocks, six Y halves instead of two and three), which the D warps were
+// waiting on, and to seven operand stages.
+template <bool F16> struct OpT;
+// kSGroups, kYSlots: depths of the S-block and Y-half rings
+// kBParts: B as hi + lo (TF32) or hi + lo + lo2 (FP16, split from the FP64
+// value: ~33 significant bits, as B's rounding error would repeat at every
+// site of a pair)
+template <> struct OpT<false> {
+  static constexpr int kStages = 5, kElem = 4, kSGroups = 2, kYSlots = 3, kBParts = 2;
+  static constexpr uint32_t kFmt = 2;  // TF32
+};
+template <> struct OpT<true> {
+  static constexpr int kStages = 6, kElem = 2, kSGroups = 4, kYSlots = 6, kBParts = 3;
+  static constexpr uint32_t kFmt = 0;  // F16
+};
+// instruction descriptor: D F32, A and B of the operand type, both K-major,
 // N = 160, M = 128
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kBtN >> 3) << 17) |
-                            ((uint32_t)(kM >> 4) << 24);
+template <bool F16>
+constexpr uint32_t idesc() {
+  return (1u << 4) | (OpT<F16>::kFmt << 7) | (OpT<F16>::kFmt << 10) | ((uint32_t)(kBtN >> 3) << 17) |
+         ((uint32_t)(kM >> 4) << 24);
+}
+constexpr uint32_t kIdesc = idesc<false>();
 
-struct __align__(1024) Smem {
+template <bool F16>
+struct __align__(1024) SmemT {
+  static constexpr int kSt = OpT<F16>::kStages;
+  static constexpr int kAPartB = kAPart * OpT<F16>::kElem, kBPartB = kBPart * OpT<F16>::kElem;  // bytes
+  static constexpr int kSGroups = OpT<F16>::kSGroups, kYSlots = OpT<F16>::kYSlots;
   float S[kSGroups][kRowsPerGroup][kRowF32];
   float Y[kYSlots][kYRows][kRowF32];
-  float A[kAStages][2][kAPart];
-  float B[kBStages][2][kBPart];
+  __align__(16) unsigned char A[kSt][2][kAPartB];
+  __align__(16) unsigned char B[kSt][OpT<F16>::kBParts][kBPartB];
   uint64_t s_full[kSGroups], s_empty[kSGroups], y_full[kYSlots], y_empty[kYSlots];
-  uint64_t a_full[kAStages], b_full[kBStages], a_empty[kAStages], b_empty[kBStages];
+  uint64_t a_full[kSt], b_full[kSt], a_empty[kSt], b_empty[kSt];
   uint64_t acc_full, folded, dotted, mma_done;
   uint32_t taddr;
   int fail;
   double red[kEWarps][2][2];
 };
-static_assert(sizeof(Smem) <= 232448, "pass-2 shared memory above the 227 KB a CTA may have");
+using Smem = SmemT<false>;
+static_assert(sizeof(SmemT<false>) <= 232448 && sizeof(SmemT<true>) <= 232448,
+              "pass-2 shared memory above the 227 KB a CTA may have");
+
+// FP16 hi and lo parts of two values, packed as the MMA reads them (the first
+// value in the low half)
+__device__ __forceinline__ void f16_split2(float a, float b, uint32_t& hi, uint32_t& lo) {
+  __half2 const h = __floats2half2_rn(a, b);
+  float2 const f = __half22float2(h);
+  __half2 const l = __floats2half2_rn(a - f.x, b - f.y);
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+// 2^(15 - e) for the smallest e with bound < 2^e: scales values bounded by
+// `bound` into FP16's range with a factor of two to spare (1 for bound 0)
+__host__ __device__ __forceinline__ float f16_scale(float bound) {
+  if (!(bound > 0.f)) return 1.f;
+  int e;
+  frexpf(bound, &e);  // bound = m 2^e, m in [0.5, 1)
+  int const k = 15 - e;
+  return ldexpf(1.f, k < -126 ? -126 : (k > 127 ? 127 : k));
+}
 
 // ---- tcgen05 / TMA helpers ---------------------------------------------------
 // shared-memory matrix descriptor, no swizzle: start, leading byte offset
@@ -132,6 +184,12 @@ __device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uin
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d),
       "l"(a), "l"(b), "r"(kIdesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_f16(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc<true>()), "r"(acc));
 }
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -350,12 +408,16 @@ static_assert(d_ph(2, 0) == 0 && d_ph(2, 1) == 2 && d_ph(2, 2) == 0 && d_ph(2, 3
 // ---- the kernel ------------------------------------------------------------------
 // kGeneric: the QED weighting from the coefficient tensor of args.coef (any
 // QED kernel, qed_provider.cuh) instead of the stand-in's closed form.
-template <bool kGeneric>
+// kF16: FP16 operands (OpT<true>); btu then holds FP16 parts and bscale the
+// B scale per (pair, flavour).
+template <bool kGeneric, bool kF16>
 __global__ void __launch_bounds__(kThreads, 1)
-p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu,
-            double* __restrict__ partials, int* __restrict__ err) {
+p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const void* __restrict__ btu,
+            const float* __restrict__ bscale, double* __restrict__ partials, int* __restrict__ err) {
+  using Sm = SmemT<kF16>;
+  constexpr int kSt = Sm::kSt, kSGroups = Sm::kSGroups, kYSlots = Sm::kYSlots;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+  Sm& sm = *reinterpret_cast<Sm*>(smem_raw);
   volatile int* fail = &sm.fail;
   int const t = threadIdx.x, warp = t >> 5, lane = t & 31;
   int const pi = blockIdx.y;
@@ -371,8 +433,8 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
   if (t == 0) {
     for (int i = 0; i < kSGroups; ++i) { mbar_init(&sm.s_full[i], 1); mbar_init(&sm.s_empty[i], kDWarps); }
     for (int i = 0; i < kYSlots; ++i) { mbar_init(&sm.y_full[i], 1); mbar_init(&sm.y_empty[i], kDGroup); }
-    for (int i = 0; i < kAStages; ++i) { mbar_init(&sm.a_full[i], kDGroup); mbar_init(&sm.a_empty[i], 1); }
-    for (int i = 0; i < kBStages; ++i) { mbar_init(&sm.b_full[i], 1); mbar_init(&sm.b_empty[i], 1); }
+    for (int i = 0; i < kSt; ++i) { mbar_init(&sm.a_full[i], kDGroup); mbar_init(&sm.a_empty[i], 1); }
+    for (int i = 0; i < kSt; ++i) { mbar_init(&sm.b_full[i], 1); mbar_init(&sm.b_empty[i], 1); }
     mbar_init(&sm.acc_full, 1);
     mbar_init(&sm.folded, kEWarps);
     mbar_init(&sm.dotted, kEWarps);
@@ -389,6 +451,15 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
   __syncthreads();
   tc_fence_after();
   uint32_t const tmem = sm.taddr;
+  // FP16: the A scale per flavour f from the tile copies' maxima, x[1 - f]
+  // (rows S) and y[f] (rows Y): |D| <= 12 |Y| |S| <= 24 max|Y| max|S|
+  float ascale0 = 1.f, ascale1 = 1.f;
+  if constexpr (kF16) {
+    const float* tx = tb.x32[pi] + f32_tile_floats(geo.V);
+    const float* ty = tb.y32 + f32_tile_floats(geo.V);
+    ascale0 = f16_scale(24.f * tx[1] * ty[0]);
+    ascale1 = f16_scale(24.f * tx[0] * ty[1]);
+  }
 
   // issue tracking for the teardown after a failure
   int rows_issued_s = -1, rows_issued_y = -1;  // last S block / Y p-block use issued
@@ -434,14 +505,15 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
       int bc = 0;
       bool ok = true;
       for (int P = 0; ok && P < nph; ++P) {
-        const float* src = btu + ((size_t)pi * 2 + (P & 1)) * kChunks * 2 * kBPart;
+        constexpr int kBP = OpT<kF16>::kBParts;
+        const unsigned char* src =
+            static_cast<const unsigned char*>(btu) + ((size_t)pi * 2 + (P & 1)) * kChunks * kBP * Sm::kBPartB;
         for (int c = 0; c < kChunks; ++c, ++bc) {
-          int const st = bc % kBStages;
-          uint64_t* const freed = kSharedEmpty ? &sm.a_empty[st] : &sm.b_empty[st];
-          if (!wait_or_fail(freed, (uint32_t)(((bc / kBStages) & 1) ^ 1), fail)) { ok = false; break; }
+          int const st = bc % kSt;
+          if (!wait_or_fail(&sm.a_empty[st], (uint32_t)(((bc / kSt) & 1) ^ 1), fail)) { ok = false; break; }
           fence_proxy_async_smem();
-          mbar_arrive_expect_tx(&sm.b_full[st], 2 * kBPart * 4);
-          bulk_g2s(sm.B[st][0], src + (size_t)c * 2 * kBPart, 2 * kBPart * 4, &sm.b_full[st]);
+          mbar_arrive_expect_tx(&sm.b_full[st], kBP * Sm::kBPartB);
+          bulk_g2s(sm.B[st][0], src + (size_t)c * kBP * Sm::kBPartB, kBP * Sm::kBPartB, &sm.b_full[st]);
           b_issued = bc;
         }
       }
@@ -456,10 +528,13 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
     if (lane == 0) {
       uint64_t const a_desc0 = sdesc(smem_u32(sm.A[0][0]), (kM / 8) * 128, 128);
       uint64_t const b_desc0 = sdesc(smem_u32(sm.B[0][0]), (kBtN / 8) * 128, 128);
-      // in 16-byte units: stage to stage, hi to lo part, k-step to k-step
-      // (two core columns: 2*16*128 and 2*20*128 bytes)
-      constexpr uint64_t kAStage16 = 2 * kAPart * 4 / 16, kALo16 = kAPart * 4 / 16, kAK16 = 2 * (kM / 8) * 128 / 16;
-      constexpr uint64_t kBStage16 = 2 * kBPart * 4 / 16, kBLo16 = kBPart * 4 / 16, kBK16 = 2 * (kBtN / 8) * 128 / 16;
+      // in 16-byte units: stage to stage, hi to lo part, and (TF32, two
+      // k-steps of 8 per chunk) k-step to k-step: two core columns, 2*16*128
+      // and 2*20*128 bytes. FP16: one k-step of 16 per chunk (the chunk's two
+      // core columns of 8 k)
+      constexpr uint64_t kAStage16 = 2 * Sm::kAPartB / 16, kALo16 = Sm::kAPartB / 16, kAK16 = 2 * (kM / 8) * 128 / 16;
+      constexpr uint64_t kBStage16 = OpT<kF16>::kBParts * Sm::kBPartB / 16, kBLo16 = Sm::kBPartB / 16,
+                         kBK16 = 2 * (kBtN / 8) * 128 / 16;
       int as = 0, bs = 0;
       uint32_t aph = 0, bph = 0;
       uint32_t const dc = tmem + kCorrCol;
@@ -483,18 +558,24 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
           uint32_t const d = c < kHalf ? d0 : d1;
           uint64_t const ahi = a_desc0 + (uint64_t)as * kAStage16, bhi = b_desc0 + (uint64_t)bs * kBStage16;
           // hi.hi into the main buffer, hi.lo and lo.hi into the correction
-          // accumulator; two k-steps of 8
-          mma_tf32(d, ahi, bhi, (c != 0 && c != kHalf) ? 1u : 0u);
-          mma_tf32(dc, ahi, bhi + kBLo16, c ? 1u : 0u);
-          mma_tf32(dc, ahi + kALo16, bhi, 1u);
-          mma_tf32(d, ahi + kAK16, bhi + kBK16, 1u);
-          mma_tf32(dc, ahi + kAK16, bhi + kBK16 + kBLo16, 1u);
-          mma_tf32(dc, ahi + kAK16 + kALo16, bhi + kBK16, 1u);
+          // accumulator
+          if constexpr (kF16) {
+            mma_f16(d, ahi, bhi, (c != 0 && c != kHalf) ? 1u : 0u);
+            mma_f16(dc, ahi, bhi + kBLo16, c ? 1u : 0u);
+            mma_f16(dc, ahi + kALo16, bhi, 1u);
+            mma_f16(dc, ahi, bhi + 2 * kBLo16, 1u);  // hi.lo2
+          } else {
+            mma_tf32(d, ahi, bhi, (c != 0 && c != kHalf) ? 1u : 0u);
+            mma_tf32(dc, ahi, bhi + kBLo16, c ? 1u : 0u);
+            mma_tf32(dc, ahi + kALo16, bhi, 1u);
+            mma_tf32(d, ahi + kAK16, bhi + kBK16, 1u);
+            mma_tf32(dc, ahi + kAK16, bhi + kBK16 + kBLo16, 1u);
+            mma_tf32(dc, ahi + kAK16 + kALo16, bhi + kBK16, 1u);
+          }
           mma_any = true;
-          mma_commit(&sm.a_empty[as]);  // with equal depths also B stage bs (= as)
-          if constexpr (!kSharedEmpty) mma_commit(&sm.b_empty[bs]);
-          if (++as == kAStages) { as = 0; aph ^= 1u; }
-          if (++bs == kBStages) { bs = 0; bph ^= 1u; }
+          mma_commit(&sm.a_empty[as]);  // also frees B stage bs (= as)
+          if (++as == kSt) { as = 0; aph ^= 1u; }
+          if (++bs == kSt) { bs = 0; bph ^= 1u; }
         }
         if (!ok) break;
         mma_commit(&sm.acc_full);
@@ -519,19 +600,21 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
         int const us = P * kBlocks + b, ss = us % kSGroups;
         if (bq == 0) ok = ok && wait_or_fail(&sm.y_full[ys], (uint32_t)((uy / kYSlots) & 1), fail);
         ok = ok && wait_or_fail(&sm.s_full[ss], (uint32_t)((us / kSGroups) & 1), fail);
-        int const ac = P * kChunks + c, as = ac % kAStages;
-        if (!ok || !wait_or_fail(&sm.a_empty[as], (uint32_t)(((ac / kAStages) & 1) ^ 1), fail)) { ok = false; break; }
+        int const ac = P * kChunks + c, as = ac % kSt;
+        if (!ok || !wait_or_fail(&sm.a_empty[as], (uint32_t)(((ac / kSt) & 1) ^ 1), fail)) { ok = false; break; }
         int const p_in = j >> 1, q_in = 2 * (j & 1);  // rows of the Y half and of the S group
-        // k = 4j .. 4j+3: core column j, the whole 16-byte row (mu*32 + s)
-        float* Ahi = sm.A[as][0] + j * 16 * 32 + s * 4;
-        float* Alo = sm.A[as][1] + j * 16 * 32 + s * 4;
+        // k = 4j .. 4j+3 of the chunk, row (mu*32 + s). TF32: core column j,
+        // the whole 16-byte row; FP16: core column j/2, its half j&1 (8 bytes)
+        unsigned char* Ahi = sm.A[as][0] + (kF16 ? (j >> 1) * 2048 + s * 16 + 8 * (j & 1) : j * 2048 + s * 16);
+        unsigned char* Alo = sm.A[as][1] + (kF16 ? (j >> 1) * 2048 + s * 16 + 8 * (j & 1) : j * 2048 + s * 16);
         if (s < nvalid) {
           if (bq == 0) {
             const float* Yr = sm.Y[ys][p_in] + f32_tile_off(s, 0);
+            float const sc = kF16 ? ((P & 1) ? ascale1 : ascale0) : 1.f;  // FP16: D scaled through Y
 #pragma unroll
             for (int c4 = 0; c4 < 6; ++c4) {
               float4 const a = *reinterpret_cast<const float4*>(Yr + c4 * 64);
-              y[4 * c4] = a.x; y[4 * c4 + 1] = a.y; y[4 * c4 + 2] = a.z; y[4 * c4 + 3] = a.w;
+              y[4 * c4] = sc * a.x; y[4 * c4 + 1] = sc * a.y; y[4 * c4 + 2] = sc * a.z; y[4 * c4 + 3] = sc * a.w;
             }
           }
           float d[4][4];  // [mu][pq0 re, pq0 im, pq1 re, pq1 im]
@@ -586,20 +669,32 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
           }
 #pragma unroll
           for (int mu = 0; mu < 4; ++mu) {
-            float4 hi, lo;
-            hi.x = tf32_round(d[mu][0]); hi.y = tf32_round(d[mu][1]);
-            hi.z = tf32_round(d[mu][2]); hi.w = tf32_round(d[mu][3]);
-            lo.x = tf32_round(d[mu][0] - hi.x); lo.y = tf32_round(d[mu][1] - hi.y);
-            lo.z = tf32_round(d[mu][2] - hi.z); lo.w = tf32_round(d[mu][3] - hi.w);
-            *reinterpret_cast<float4*>(Ahi + mu * 4 * 32) = hi;
-            *reinterpret_cast<float4*>(Alo + mu * 4 * 32) = lo;
+            if constexpr (kF16) {
+              uint2 hi, lo;
+              f16_split2(d[mu][0], d[mu][1], hi.x, lo.x);
+              f16_split2(d[mu][2], d[mu][3], hi.y, lo.y);
+              *reinterpret_cast<uint2*>(Ahi + mu * 32 * 16) = hi;
+              *reinterpret_cast<uint2*>(Alo + mu * 32 * 16) = lo;
+            } else {
+              float4 hi, lo;
+              hi.x = tf32_round(d[mu][0]); hi.y = tf32_round(d[mu][1]);
+              hi.z = tf32_round(d[mu][2]); hi.w = tf32_round(d[mu][3]);
+              lo.x = tf32_round(d[mu][0] - hi.x); lo.y = tf32_round(d[mu][1] - hi.y);
+              lo.z = tf32_round(d[mu][2] - hi.z); lo.w = tf32_round(d[mu][3] - hi.w);
+              *reinterpret_cast<float4*>(Ahi + mu * 32 * 16) = hi;
+              *reinterpret_cast<float4*>(Alo + mu * 32 * 16) = lo;
+            }
           }
         } else {
-          float4 const z = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
           for (int mu = 0; mu < 4; ++mu) {
-            *reinterpret_cast<float4*>(Ahi + mu * 4 * 32) = z;
-            *reinterpret_cast<float4*>(Alo + mu * 4 * 32) = z;
+            if constexpr (kF16) {
+              *reinterpret_cast<uint2*>(Ahi + mu * 32 * 16) = make_uint2(0u, 0u);
+              *reinterpret_cast<uint2*>(Alo + mu * 32 * 16) = make_uint2(0u, 0u);
+            } else {
+              *reinterpret_cast<float4*>(Ahi + mu * 32 * 16) = make_float4(0.f, 0.f, 0.f, 0.f);
+              *reinterpret_cast<float4*>(Alo + mu * 32 * 16) = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
           }
         }
         fence_proxy_async_smem();
@@ -683,6 +778,7 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&sm.dotted);
+      if constexpr (kF16) a *= 1.f / (((P & 1) ? ascale1 : ascale0) * bscale[2 * pi + (P & 1)]);  // powers of two: exact
       if (valid) {
         if (P & 1) run1.add(-(double)a);
         else run0.add(-(double)a);
@@ -718,8 +814,8 @@ p2tc_kernel(TcBatch tb, Geometry geo, P2Args args, const float* __restrict__ btu
         if (u >= 0) mbar_wait(&sm.y_full[u % kYSlots], (uint32_t)((u / kYSlots) & 1));
     }
     if (warp == kWarpB && lane == 0)
-      for (int u = b_issued - kBStages + 1; u <= b_issued; ++u)
-        if (u >= 0) mbar_wait(&sm.b_full[u % kBStages], (uint32_t)((u / kBStages) & 1));
+      for (int u = b_issued - kSt + 1; u <= b_issued; ++u)
+        if (u >= 0) mbar_wait(&sm.b_full[u % kSt], (uint32_t)((u / kSt) & 1));
     if (warp == kWarpMma && lane == 0 && mma_any) {
       mma_commit(&sm.mma_done);
       mbar_wait(&sm.mma_done, 0);
@@ -776,41 +872,112 @@ __global__ void btu_build_kernel(const double* __restrict__ g, int nf, float* __
   btu[base + kBPart + off] = lo;
 }
 
+// FP16 operands: the B scale per (pair, flavour), 2^(15 - e) with 2^e above
+// max |g| (every Bt entry is a component of g times a power of i)
+__global__ void bscale_kernel(const double* __restrict__ g, int nf, float* __restrict__ bscale) {
+  __shared__ float red[8];
+  int const fl = blockIdx.x, pi = blockIdx.y;
+  const double* gp = g + ((size_t)pi * nf + fl) * kGLen;
+  float m = 0.f;
+  for (int i = threadIdx.x; i < kGLen; i += blockDim.x) m = fmaxf(m, fabsf((float)gp[i]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
+    bscale[pi * 2 + fl] = f16_scale(m);
+  }
+}
+
+// btu_build_kernel's values scaled by bscale, as FP16 hi, lo and lo2 parts
+// (each the rounding of the rest of the FP64 value) in the K-major
+// core-matrix layout of 8 k (core (k/8, n/8) at (k/8*20 + n/8)*128
+// bytes, row n%8 at 16 bytes, k%8 at 2 bytes)
+__global__ void btu16_build_kernel(const double* __restrict__ g, int nf, const float* __restrict__ bscale,
+                                   __half* __restrict__ btu) {
+  int const fl = blockIdx.y, pi = blockIdx.z;
+  int const i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kBtK * kBtN || fl >= nf) return;
+  const double* g_dzu = g + ((size_t)pi * nf + fl) * kGLen;
+  const double* g_dzsu = g_dzu + kGDzuLen;
+  int const k = i / kBtN, n = i % kBtN;
+  int const cc = k / kKc, kl = k % kKc, jj = kl >> 2, hh = (kl >> 1) & 1, e = kl & 1;
+  int const bb = cc >> 1, bbp = bb / kBlocksQ, bbq = bb - bbp * kBlocksQ;
+  int const p = 4 * bbp + 2 * (cc & 1) + (jj >> 1), q = 4 * bbq + 2 * (jj & 1) + hh;
+  int const lam = n & 3, nu = (n >> 2) & 3, j = n >> 4;
+  int const sq = q / 3, cq = q % 3;
+  int sq2 = 0;
+#pragma unroll
+  for (int s = 0; s < 4; ++s)
+    if (gg5_src(lam, s) == sq) sq2 = s;
+  int const ph = gg5_ph(lam, sq2);
+  const double* v = j < 6 ? g_dzu + ((((j * 4 + nu) * 12) + (3 * sq2 + cq)) * 12 + p) * 2
+                          : g_dzsu + (((((j - 6) * 4 + nu) * 12) + (3 * sq2 + cq)) * 12 + p) * 2;
+  double re, im;
+  mul_iph(ph, v[0], v[1], re, im);
+  double const x = (e == 0 ? re : -im) * (double)bscale[pi * 2 + fl];  // a power of two: exact
+  __half const hi = __double2half(x);
+  double const r1 = x - (double)__half2float(hi);
+  __half const lo = __double2half(r1);
+  __half const lo2 = __double2half(r1 - (double)__half2float(lo));
+  int const off = ((kl >> 3) * (kBtN / 8) + (n >> 3)) * 64 + (n & 7) * 8 + (kl & 7);
+  size_t const base = (((size_t)pi * 2 + fl) * kChunks + cc) * 3 * kBPart;
+  btu[base + off] = hi;
+  btu[base + kBPart + off] = lo;
+  btu[base + 2 * kBPart + off] = lo2;
+}
+
 }  // namespace tc
 
 size_t tc_smem_bytes() { return sizeof(tc::Smem); }
 int tc_threads() { return tc::kThreads; }
 size_t tc_btu_floats_per_pair() { return (size_t)2 * tc::kChunks * 2 * tc::kBPart; }
 
-int tc_init(int nsm, int& grid) {
-  cudaError_t e = cudaFuncSetAttribute(tc::p2tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)sizeof(tc::Smem));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(tc::p2tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sizeof(tc::Smem));
+template <bool G, bool F>
+static int tc_init_one(int& nb) {
+  size_t const smem = sizeof(tc::SmemT<F>);
+  cudaError_t e = cudaFuncSetAttribute(tc::p2tc_kernel<G, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_fail(e, "p2tc smem attribute");
-  int nb = 0, nbg = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tc::p2tc_kernel<false>, tc::kThreads, sizeof(tc::Smem));
-  if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbg, tc::p2tc_kernel<true>, tc::kThreads, sizeof(tc::Smem));
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tc::p2tc_kernel<G, F>, tc::kThreads, smem);
   if (e != cudaSuccess) return cuda_fail(e, "p2tc occupancy");
-  if (nb < 1 || nbg < 1) return fail(HLBL_ECUDA, "p2tc kernel cannot be resident (smem %zu)", sizeof(tc::Smem));
+  if (nb < 1) return fail(HLBL_ECUDA, "p2tc kernel cannot be resident (smem %zu)", smem);
+  return HLBL_OK;
+}
+
+int tc_init(int nsm, int& grid) {
+  int nb = 0;
+  if (int rc = tc_init_one<false, false>(nb)) return rc;
+  if (int rc = tc_init_one<true, false>(nb)) return rc;
+  if (int rc = tc_init_one<false, true>(nb)) return rc;
+  if (int rc = tc_init_one<true, true>(nb)) return rc;
   // one CTA per SM: each allocates all 512 TMEM columns
   grid = nsm;
   return HLBL_OK;
 }
 
-void tc_launch_btu(const double* d_g, int npairs, float* d_btu, cudaStream_t st) {
+void tc_launch_btu(const double* d_g, int npairs, void* d_btu, bool f16, float* d_bscale, cudaStream_t st) {
   dim3 const gb((kBtK * kBtN + 255) / 256, 2, npairs);
-  tc::btu_build_kernel<<<gb, 256, 0, st>>>(d_g, 2, d_btu);
+  if (f16) {
+    tc::bscale_kernel<<<dim3(2, npairs), 256, 0, st>>>(d_g, 2, d_bscale);
+    tc::btu16_build_kernel<<<gb, 256, 0, st>>>(d_g, 2, d_bscale, static_cast<__half*>(d_btu));
+  } else {
+    tc::btu_build_kernel<<<gb, 256, 0, st>>>(d_g, 2, static_cast<float*>(d_btu));
+  }
 }
 
 void tc_launch_p2(int grid, int npairs, cudaStream_t st, const TcBatch& tb, const Geometry& geo,
-                  const P2Args& a, const float* d_btu, double* partials, int* err) {
-  if (a.coef)
-    tc::p2tc_kernel<true><<<dim3(grid, npairs), tc::kThreads, sizeof(tc::Smem), st>>>(tb, geo, a, d_btu, partials, err);
-  else
-    tc::p2tc_kernel<false><<<dim3(grid, npairs), tc::kThreads, sizeof(tc::Smem), st>>>(tb, geo, a, d_btu, partials, err);
+                  const P2Args& a, const void* d_btu, bool f16, const float* d_bscale, double* partials, int* err) {
+  dim3 const gr(grid, npairs);
+  if (f16) {
+    size_t const smem = sizeof(tc::SmemT<true>);
+    if (a.coef) tc::p2tc_kernel<true, true><<<gr, tc::kThreads, smem, st>>>(tb, geo, a, d_btu, d_bscale, partials, err);
+    else tc::p2tc_kernel<false, true><<<gr, tc::kThreads, smem, st>>>(tb, geo, a, d_btu, d_bscale, partials, err);
+  } else {
+    size_t const smem = sizeof(tc::SmemT<false>);
+    if (a.coef) tc::p2tc_kernel<true, false><<<gr, tc::kThreads, smem, st>>>(tb, geo, a, d_btu, d_bscale, partials, err);
+    else tc::p2tc_kernel<false, false><<<gr, tc::kThreads, smem, st>>>(tb, geo, a, d_btu, d_bscale, partials, err);
+  }
 }
 
 long long tc_tiles(long long V) { return (V + tc::kSites - 1) / tc::kSites; }

@@ -127,8 +127,10 @@ int hlbl_autotune(hlbl_ctx* ctx, const double* d_fwd_y, int n, const double* con
  * d_out[f][ia][tile][half][6][16][4] floats, tiles of 32 sites ((V + 31) / 32
  * of them, the last padded and its pad left untouched) in two halves of 16, a
  * site's 24 sink components as six groups of 4; each value rounded to
- * nearest even from FP64. 2 * 12 * tiles * 768 floats. Asynchronous on the
- * context's stream. No counterpart in the reference. */
+ * nearest even from FP64, 2 * 12 * tiles * 768 floats, then a trailer of 32
+ * floats whose first two hold the largest magnitude of flavour 0 and 1
+ * (hlbl_f32_block_length floats in all). Asynchronous on the context's
+ * stream. No counterpart in the reference. */
 int hlbl_f32_tile_copy(hlbl_ctx* ctx, const double* d_block, float* d_out);
 
 /* Floats in one FP32 tile copy of a block of the context's lattice. */
@@ -169,6 +171,14 @@ int hlbl_ctx_set_qed_fp32(hlbl_ctx* ctx, int on, double r64);
  * by pass 1) or on the CUDA cores (on = 0). No counterpart in the
  * reference. */
 int hlbl_ctx_set_tensor_cores(hlbl_ctx* ctx, int on);
+
+/* Operands of the FP32-copy path's tensor-core pass 2 (hlbl_kernel_sums_batched_f32):
+ * on = 1 (the default), FP16: the same hi + lo split as 3xTF32 (22
+ * significant bits) in half the bytes and half the MMAs, with power-of-two
+ * scales from the largest magnitudes the tile copies carry, so the copies
+ * must come from hlbl_f32_tile_copy; on = 0, TF32. No counterpart in the
+ * reference. */
+int hlbl_ctx_set_tc_fp16(hlbl_ctx* ctx, int on);
 
 /* One CUDA graph per window: every asynchronous call made on the context
  * between hlbl_graph_begin and hlbl_graph_end (typically one

@@ -110,23 +110,31 @@ def test_f32_tile_copy_rounds_like_ieee_and_lays_out_tiles():
     blk[:edge.size] = edge
     blk[1000:1000 + edge.size] = edge * 3.0
     nt = (V + 31) // 32
-    out = torch.full((2 * 12 * nt * 768,), float("nan"), dtype=torch.float32, device="cuda")
     with hg.Contractor(lat) as c:
+        assert c.f32_block_length == 2 * 12 * nt * 768 + 32  # the tiles, then the trailer
+        out = torch.full((c.f32_block_length,), float("nan"), dtype=torch.float32, device="cuda")
         c.f32_tile_copy(dev(blk), out)
         c.check()
-    got = out.cpu().numpy().reshape(2 * 12, nt, 2, 6, 16, 4)
+    full = out.cpu().numpy()
+    got = full[:2 * 12 * nt * 768].reshape(2 * 12, nt, 2, 6, 16, 4)
     want = blk.astype(np.float32).reshape(2 * 12, V, 6, 4)
     for site in range(V):
         a = got[:, site // 32, (site % 32) // 16, :, site % 16, :]
         assert np.array_equal(a.view(np.uint32), want[:, site].view(np.uint32)), site
+    # the trailer: the largest magnitude per flavour (here infinities were planted)
+    trailer = full[2 * 12 * nt * 768:]
+    for f in range(2):
+        assert trailer[f] == np.max(np.abs(want[12 * f:12 * f + 12])), (f, trailer[f])
 
 
+@pytest.mark.parametrize("fp16", [False, True])
 @pytest.mark.parametrize("lat", [(6, 4, 4, 4), (3, 5, 1, 7)])
-def test_f32_copy_path_matches_oracle_and_fp64_input_path(lat):
+def test_f32_copy_path_matches_oracle_and_fp64_input_path(lat, fp16):
     """hlbl_kernel_sums_batched_f32 on FP32 tile copies made once per block
-    (hlbl_f32_tile_copy): within 1e-4 of the oracle and within FP32 accuracy
-    (1e-5 at the pair's scale; pass 1's tiling differs) of the same batch on
-    the FP64 blocks; the autotuner's choice stays within the same bars."""
+    (hlbl_f32_tile_copy), with TF32 or FP16 operands in pass 2: within 1e-4
+    of the oracle and within FP32 accuracy (1e-5 at the pair's scale; pass 1's
+    tiling differs) of the same batch on the FP64 blocks; the autotuner's
+    choice stays within the same bars."""
     import hlbl_gb300 as hg
 
     xu = hg.xunit(105.658, 0.1)
@@ -135,6 +143,7 @@ def test_f32_copy_path_matches_oracle_and_fp64_input_path(lat):
     gsxs = [tuple((i + r) % L for r, L in enumerate(lat)) for i in range(3)]
     yvs = [(1, 0, -1, 1), (0, 1, 1, -1), (2, -1, 0, 0)]
     with hg.Contractor(lat) as c:
+        c.set_tc_fp16(fp16)
         d_y, d_srcs = dev(y), [dev(s) for s in srcs]
         n32 = c.f32_block_length
         y32 = torch.empty(n32, dtype=torch.float32, device="cuda")
@@ -171,13 +180,15 @@ def test_f32_copy_path_matches_oracle_and_fp64_input_path(lat):
         assert S.pair_rel_err(got[i], r64[i]) <= 1e-5
 
 
+@pytest.mark.parametrize("fp16", [False, True])
 @pytest.mark.parametrize("lat", [(8, 8, 8, 24), (4, 6, 5, 21), (5, 3, 7, 40)])
-def test_f32_copy_pass1_over_many_tiles(lat):
+def test_f32_copy_pass1_over_many_tiles(lat, fp16):
     """Every pass-1 variant of the FP32-copy path on lattices with several
     16-site tiles per CTA and runs along z that cross tiles (LZ = 24, 21, 40;
-    odd extents, whose zero-half point is not L/2 of an even L): each pair
-    against the oracle (1e-4) and against the FP64 path at FP32 accuracy
-    (1e-5 at the pair's scale), repeatable bit for bit."""
+    odd extents, whose zero-half point is not L/2 of an even L), pass 2 with
+    TF32 or FP16 operands: each pair against the oracle (1e-4) and against
+    the FP64 path at FP32 accuracy (1e-5 at the pair's scale), repeatable bit
+    for bit."""
     import hlbl_gb300 as hg
 
     xu = hg.xunit(105.658, 0.1)
@@ -186,6 +197,7 @@ def test_f32_copy_pass1_over_many_tiles(lat):
     gsxs = [(1, 2, 3, 5), tuple(L - 1 for L in lat)]
     yvs = [(1, -1, 2, -3), (0, 2, -1, 7)]
     with hg.Contractor(lat) as c:
+        c.set_tc_fp16(fp16)
         d_y, d_srcs = dev(y), [dev(s) for s in srcs]
         n32 = c.f32_block_length
         y32 = torch.empty(n32, dtype=torch.float32, device="cuda")
@@ -212,3 +224,38 @@ def test_f32_copy_pass1_over_many_tiles(lat):
         for v in range(4):
             assert S.pair_rel_err(res[v][i], orc) <= TOL32
             assert S.pair_rel_err(res[v][i], r64[i]) <= 1e-5, (v, res[v][i], r64[i])
+
+
+def test_fp16_operands_over_scales():
+    """FP16 operands on blocks of very different magnitudes (1e-12, 1, 1e9 and
+    a block whose flavours differ by 1e6): the power-of-two scales keep every
+    pair within FP32 accuracy of the TF32 operands (1e-5 at the pair's scale)
+    and within 1e-4 of the oracle."""
+    import hlbl_gb300 as hg
+
+    lat = (6, 4, 4, 8)
+    xu = hg.xunit(105.658, 0.1)
+    base_y = S.gaussian_block(lat, 301)
+    base_x = S.gaussian_block(lat, 302)
+    half = base_y.size // 2
+    cases = [(1e-12, 1.0), (1.0, 1e9), (1e-3, 1e3)]
+    with hg.Contractor(lat) as c:
+        n32 = c.f32_block_length
+        for sy, sx in cases:
+            y = base_y * sy
+            x = base_x * sx
+            x[half:] *= 1e-6  # flavour 1 of the partner far smaller than flavour 0
+            y32 = torch.empty(n32, dtype=torch.float32, device="cuda")
+            x32 = torch.empty(n32, dtype=torch.float32, device="cuda")
+            c.f32_tile_copy(dev(y), y32)
+            c.f32_tile_copy(dev(x), x32)
+            res = {}
+            for fp16 in (False, True):
+                c.set_tc_fp16(fp16)
+                o = torch.zeros((1, 2), dtype=torch.float64, device="cuda")
+                c.kernel_sums_batched_f32(y32, [x32], [(1, 2, 3, 4)], [(2, -1, 1, 3)], xu, o)
+                c.check()
+                res[fp16] = o.cpu().numpy()[0]
+            orc = S.oracle_kernel_sum(x, y, (1, 2, 3, 4), (2, -1, 1, 3), xu, lat)
+            assert S.pair_rel_err(res[True], orc) <= TOL32, (sy, sx, res[True], orc)
+            assert S.pair_rel_err(res[True], res[False]) <= 1e-5, (sy, sx, res)
