@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--c2-ref-pairs", type=int, default=8)
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="skip the baseline leg of the reference's own kernels on the GPU")
+    ap.add_argument("--tc-tf32", action="store_true",
+                    help="TF32 operands in the tensor-core pass 2 instead of FP16 (the library's default)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default kernel variants (profiling: the first launches are the timed ones)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -263,6 +265,8 @@ def main():
     warm, timed = order[:args.warmup], order[args.warmup:]
 
     c = hg.Contractor(LATTICE, device=local_rank)
+    p2_fp16 = not args.tc_tf32
+    c.set_tc_fp16(p2_fp16)
     stream = torch.cuda.Stream()
     c.set_stream(stream)
     blocks = {}
@@ -614,7 +618,8 @@ def main():
     p1_bytes = sum((1 + gi) for gi in groups) * blk * 0.5 / max(1, p1n)  # FP32 copies read
     p1_gbs = p1_bytes / (p1_avg_ms * 1e-3) / 1e9
     # pass 2, per pair: the 128 x 160 x 288 product per 32 sites per flavour
-    # (FMA = 2 flops), algorithmic; the tensor cores issue 3x (3xTF32)
+    # (FMA = 2 flops), algorithmic; the tensor cores issue 4x (FP16 operands)
+    # or 3x (3xTF32)
     gemm_flop_pair = 2 * 2 * V * 4 * 288 * 160
     p2_tflops = gemm_flop_pair * n_prof / max(1, p2n) / (p2_avg_ms * 1e-3) / 1e12
     p2_bytes = sum((1 + gi) for gi in groups) * blk * 0.5 / max(1, p2n)  # FP32 tile copies read
@@ -624,12 +629,23 @@ def main():
              "traffic": traffic_per_launch("p1_bytes_per_launch", p1n),
              "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
              "kernel_ms": round(p1_avg_ms, 3), "bytes_per_launch": p1_bytes}
-    rl_p2 = {"bound": "tensor", "kernel": f"pass 2, {tune['p2']} (batched)",
-             "achieved": round(p2_tflops, 2), "peak": round(tf32_peak, 1), "unit": "TFLOP/s",
-             "frac": round(p2_tflops / tf32_peak, 5),
+    # pass 2's operands are FP16 (the default: four FP16 MMAs per product,
+    # hi.hi + hi.lo + lo.hi + hi.lo2) against the measured dense 16-bit GEMM
+    # rate (bf16 and fp16 run at the same rate), or TF32 (three) against a
+    # cuBLAS TF32 GEMM measured here
+    if p2_fp16:
+        p2_peak, p2_issue = peaks["bf16_tflops"], 4
+        p2_peak_src = f"{peak_src} (MEASURED_PEAKS.json bf16_tflops: dense 16-bit GEMM, burst; FP16 operands)"
+    else:
+        p2_peak, p2_issue = tf32_peak, 3
+        p2_peak_src = "measured here: cuBLAS TF32 GEMM 8192^3 (torch.matmul, allow_tf32); TF32 operands"
+    rl_p2 = {"bound": "tensor", "kernel": f"pass 2, {tune['p2']}, {'FP16' if p2_fp16 else 'TF32'} operands (batched)",
+             "achieved": round(p2_tflops, 2), "peak": round(p2_peak, 1), "unit": "TFLOP/s",
+             "frac": round(p2_tflops / p2_peak, 5),
              "traffic": traffic_per_launch("p2_bytes_per_launch", p2n),
-             "peak_source": "measured here: cuBLAS TF32 GEMM 8192^3 (torch.matmul, allow_tf32)",
-             "issued_tf32_tflops": round(3 * p2_tflops, 2), "kernel_ms": round(p2_avg_ms, 3),
+             "peak_source": p2_peak_src,
+             "issued_tflops": round(p2_issue * p2_tflops, 2), "issued_per_product": p2_issue,
+             "tf32_gemm_tflops_measured": round(tf32_peak, 1), "kernel_ms": round(p2_avg_ms, 3),
              "hbm_gbs": round(p2_bytes / (p2_avg_ms * 1e-3) / 1e9, 2)}
     dominant = rl_p1 if p1_avg_ms >= p2_avg_ms else rl_p2
 
@@ -652,7 +668,9 @@ def main():
                    "lattice": list(LATTICE), "pairs_timed": n32,
                    "path": "batched per source (autotuned), one CUDA graph for the timed sources; "
                            "blocks as FP32 tile copies (each new block converted once, in its step); "
-                           "FP32 products (pass 2 on the tensor cores, 3xTF32), FP64 sums",
+                           + ("FP32 products (pass 2 on the tensor cores, FP16 operands split hi/lo with power-of-two "
+                              "scales), FP64 sums" if p2_fp16
+                              else "FP32 products (pass 2 on the tensor cores, 3xTF32), FP64 sums"),
                    "qed_weight": "stand-in (KQED unavailable), exact: FP32 quadrature, FP64 within "
                                  "0.1/m_mu of the origin; the learned weight is the 'surrogate' line",
                    "l2": "inputs 3.06 GB per block, larger than L2; no flush"},
