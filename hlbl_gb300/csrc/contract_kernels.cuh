@@ -242,7 +242,7 @@ p1_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, int f0,
     }
     for (int s = t; s < TS; s += blockDim.x) {
       int rel[4];
-      rel_coords(geo, gsx, min(s0 + s, geo.V - 1), rel);
+      rel_coords_fast(geo, gsx, min(s0 + s, geo.V - 1), rel);
 #pragma unroll
       for (int r = 0; r < 4; ++r) s_zh[s * 4 + r] = (T)coord_map_zerohalf(rel[r], geo.global[r]);
     }
@@ -756,7 +756,7 @@ p2_kernel(const double* __restrict__ y, PairBatch batch, Geometry geo, P2Args ar
     for (int it = t; it < TS * 4; it += nthr) {
       int const s = it >> 2, r = it & 3;
       int rel[4];
-      rel_coords(geo, gsx, min(s0 + s, geo.V - 1), rel);
+      rel_coords_fast(geo, gsx, min(s0 + s, geo.V - 1), rel);
       s_vec[s * 12 + r] = coord_map(rel[r], geo.global[r]) * xu;
       s_vec[s * 12 + 4 + r] = coord_map_diff(rel[r], yv[r], geo.global[r]) * xu;
       s_vec[s * 12 + 8 + r] = (double)coord_map_zerohalf(rel[r], geo.global[r]);

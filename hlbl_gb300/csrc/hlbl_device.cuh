@@ -91,6 +91,26 @@ __device__ __forceinline__ void rel_coords(const Geometry& g, const int gsx[4], 
   }
 }
 
+// The same with 32-bit divisions (a handful of instructions each instead of a
+// 64-bit division's few dozen) where the volume allows it.
+__device__ __forceinline__ void rel_coords_fast(const Geometry& g, const int gsx[4], long long site, int rel[4]) {
+  if (g.V > 0xFFFFFFFFLL) {
+    rel_coords(g, gsx, site, rel);
+    return;
+  }
+  unsigned s = (unsigned)site;
+  int c[4];
+  c[3] = (int)(s % (unsigned)g.local[3]); s /= (unsigned)g.local[3];
+  c[2] = (int)(s % (unsigned)g.local[2]); s /= (unsigned)g.local[2];
+  c[1] = (int)(s % (unsigned)g.local[1]); s /= (unsigned)g.local[1];
+  c[0] = (int)s;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    int const v = c[r] + g.pc[r] * g.local[r] - gsx[r];
+    rel[r] = (v + g.global[r]) % g.global[r];
+  }
+}
+
 // ---- TMA bulk copies and mbarriers ----------------------------------------
 // Tiles of propagator rows are staged with cp.async.bulk (1-D TMA): one
 // thread issues a copy per contiguous row run and the mbarrier's transaction

@@ -188,11 +188,13 @@ p1f32_kernel(TcBatch tb, Geometry geo, double* __restrict__ partials, int* __res
     const float* Brow = sm.stage[st][NFL == 1 ? 12 + ib : 24 + fl * 12 + ib];
     long long const s0 = tile * kTS;
     int const nvalid = (int)min((long long)kTS, geo.V - s0);
-    for (int it = t; it < kTS * 4; it += blockDim.x) {
-      int const s = it >> 2, r = it & 3;
+    // a thread per site (its four weights), 32-bit index arithmetic: this
+    // work falls on one warp and every warp waits for it at the barrier
+    for (int s = t; s < kTS; s += blockDim.x) {
       int rel[4];
-      rel_coords(geo, gsx, min(s0 + s, geo.V - 1), rel);
-      sm.zh[s][r] = (float)coord_map_zerohalf(rel[r], geo.global[r]);
+      rel_coords_fast(geo, gsx, min(s0 + s, geo.V - 1), rel);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) sm.zh[s][r] = (float)coord_map_zerohalf(rel[r], geo.global[r]);
     }
     if (!mbar_wait(&s_bar[st], parity)) s_fail = 1;
     __syncthreads();
@@ -287,11 +289,11 @@ p1f32_ws_kernel(TcBatch tb, Geometry geo, double* __restrict__ partials, int* __
       }
       if (*fail) break;
       long long const s0 = tile * kTS;
-      for (int i = lane; i < kTS * 4; i += 32) {
-        int const s = i >> 2, r = i & 3;
+      for (int s = lane; s < kTS; s += 32) {
         int rel[4];
-        rel_coords(geo, gsx, min(s0 + s, geo.V - 1), rel);
-        sm.zh[st][s][r] = (float)coord_map_zerohalf(rel[r], geo.global[r]);
+        rel_coords_fast(geo, gsx, min(s0 + s, geo.V - 1), rel);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) sm.zh[st][s][r] = (float)coord_map_zerohalf(rel[r], geo.global[r]);
       }
       if (lane == 0) {
         fence_proxy_async_smem();

@@ -152,7 +152,7 @@ __device__ __forceinline__ void f16_split2(float a, float b, uint32_t& hi, uint3
 // 2^(15 - e) for the smallest e with bound < 2^e: scales values bounded by
 // `bound` into FP16's range with a factor of two to spare (1 for bound 0)
 __host__ __device__ __forceinline__ float f16_scale(float bound) {
-  if (!(bound > 0.f)) return 1.f;
+  if (!(bound > 0.f) || !(bound <= 3.0e38f)) return 1.f;  // zero, NaN or infinite inputs
   int e;
   frexpf(bound, &e);  // bound = m 2^e, m in [0.5, 1)
   int const k = 15 - e;
