@@ -131,7 +131,7 @@ __device__ __forceinline__ void tile_sums(const float* __restrict__ Arow, const 
 template <int ST, int NFL>
 struct Smem {
   float stage[ST][rows<NFL>()][kRowStride];
-  float zh[kTS][4];
+  float zh[2][kTS][4];  // this tile's zero-half weights and the next one's
 };
 
 template <int ST, int NFL>
@@ -172,15 +172,35 @@ p1f32_kernel(TcBatch tb, Geometry geo, double* __restrict__ partials, int* __res
   __syncthreads();
 
   KahanF acc_u[6][2], acc_s[4][2];
+  // a tile's zero-half weights, a thread per site (its four), with 32-bit
+  // index arithmetic where the volume allows it
+  bool const small = geo.V <= 0xFFFFFFFFLL;
+  auto zh_fill = [&](long long tl, int buf) {
+    long long const s0 = tl * kTS;
+    for (int s = t; s < kTS; s += blockDim.x) {
+      int rel[4];
+      rel_coords_fast(geo, gsx, min(s0 + s, geo.V - 1), rel);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) sm.zh[buf][s][r] = (float)coord_map_zerohalf(rel[r], geo.global[r]);
+    }
+  };
   long long tile = blockIdx.x;
-  if (t == 0 && tile < ntiles) issue(tile, 0);
+  if (tile < ntiles) {
+    if (t == 0) issue(tile, 0);
+    zh_fill(tile, 0);
+  }
+  __syncthreads();
+  // one block barrier per tile: the next tile's weights are written (into the
+  // other zh buffer) before it, and the stage and zh buffer of this tile are
+  // rewritten only after the next one
   int it = 0;
   for (; tile < ntiles; tile += gridDim.x, ++it) {
-    int const st = ST == 1 ? 0 : (it & 1);
+    int const st = ST == 1 ? 0 : (it & 1), zb = it & 1;
     uint32_t const parity = ST == 1 ? (uint32_t)(it & 1) : (uint32_t)((it >> 1) & 1);
+    bool const more = tile + gridDim.x < ntiles;
     // ST = 2: prefetch the next tile into the other stage (its readers passed
     // the previous iteration's barrier)
-    if (ST == 2 && t == 0 && tile + gridDim.x < ntiles) {
+    if (ST == 2 && t == 0 && more) {
       fence_proxy_async_smem();
       issue(tile + gridDim.x, st ^ 1);
     }
@@ -188,20 +208,13 @@ p1f32_kernel(TcBatch tb, Geometry geo, double* __restrict__ partials, int* __res
     const float* Brow = sm.stage[st][NFL == 1 ? 12 + ib : 24 + fl * 12 + ib];
     long long const s0 = tile * kTS;
     int const nvalid = (int)min((long long)kTS, geo.V - s0);
-    // a thread per site (its four weights), 32-bit index arithmetic: this
-    // work falls on one warp and every warp waits for it at the barrier
-    for (int s = t; s < kTS; s += blockDim.x) {
-      int rel[4];
-      rel_coords_fast(geo, gsx, min(s0 + s, geo.V - 1), rel);
-#pragma unroll
-      for (int r = 0; r < 4; ++r) sm.zh[s][r] = (float)coord_map_zerohalf(rel[r], geo.global[r]);
-    }
-    if (!mbar_wait(&s_bar[st], parity)) s_fail = 1;
-    __syncthreads();
+    int const z0 = small ? (int)((unsigned)s0 % (unsigned)geo.local[3]) : (int)(s0 % geo.local[3]);
+    if (mbar_wait(&s_bar[st], parity)) tile_sums(Arow, Brow, sm.zh[zb], nvalid, z0, geo.local[3], acc_u, acc_s);
+    else s_fail = 1;
+    if (more) zh_fill(tile + gridDim.x, zb ^ 1);
+    __syncthreads();  // the stage and zh[zb] are rewritten after this
     if (s_fail) break;
-    tile_sums(Arow, Brow, sm.zh, nvalid, (int)(s0 % geo.local[3]), geo.local[3], acc_u, acc_s);
-    __syncthreads();  // the stage and zh are rewritten for the next tile
-    if (ST == 1 && t == 0 && tile + gridDim.x < ntiles) {
+    if (ST == 1 && t == 0 && more) {
       fence_proxy_async_smem();
       issue(tile + gridDim.x, 0);
     }
