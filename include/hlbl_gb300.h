@@ -167,9 +167,10 @@ int hlbl_ctx_set_p1f32_variant(hlbl_ctx* ctx, int variant, int group);
 int hlbl_ctx_set_qed_fp32(hlbl_ctx* ctx, int on, double r64);
 
 /* FP32 two-flavour pass 2 on the tensor cores (on = 1, the default:
- * tcgen05 MMAs with 3xTF32 products, FP32 tile copies of the blocks written
- * by pass 1) or on the CUDA cores (on = 0). No counterpart in the
- * reference. */
+ * tcgen05 MMAs with split hi + lo products, FP32 tile copies of the blocks
+ * written by pass 1 or by hlbl_f32_tile_copy; the operand type as
+ * hlbl_ctx_set_tc_fp16 sets it, TF32 for FP64 blocks) or on the CUDA cores
+ * (on = 0). No counterpart in the reference. */
 int hlbl_ctx_set_tensor_cores(hlbl_ctx* ctx, int on);
 
 /* Operands of the FP32-copy path's tensor-core pass 2 (hlbl_kernel_sums_batched_f32):
